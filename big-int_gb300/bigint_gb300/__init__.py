@@ -1,0 +1,233 @@
+"""Python front end of the GB300 batched big-integer library.
+
+A thin ctypes layer over ``libbigint_gb300.so`` (the C ABI declared in
+``include/bigint_gb300.h``).  It exists for tests, benchmarks and Python
+callers; C, C++ and other FFI users bind the shared library directly.
+
+Device functions take CUDA tensors of shape ``[n, m]`` whose element size is 4
+(u32 limbs) or 8 (u64 limbs) -- any integer dtype of that size, e.g.
+``torch.int64`` holding the bits of u64 limbs -- and run on the current torch
+stream unless ``stream`` is given.  Host functions take numpy ``uint32`` /
+``uint64`` arrays and mirror the reference's synchronous host wrappers.
+
+There is no CPU fallback: if the shared library is missing or fails to load,
+every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import _build
+from . import workloads  # noqa: F401  (seeded synthetic inputs)
+
+LIB_PATH = _build.LIB_PATH
+
+_lib = None
+
+STATUS = {
+    0: "BI_OK",
+    1: "BI_EINVAL",
+    2: "BI_EDIV0",
+    3: "BI_ENOMEM",
+    4: "BI_ETIMEDOUT",
+    5: "BI_ECUDA",
+    6: "BI_EUNSUPPORTED",
+}
+
+
+class BigIntError(RuntimeError):
+    def __init__(self, status: int, detail: str):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {detail}")
+
+
+def build(force: bool = False, verbose: bool = False) -> str:
+    return _build.build(force=force, verbose=verbose)
+
+
+def lib() -> ctypes.CDLL:
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with bigint_gb300.build() "
+            "(there is no CPU fallback)"
+        )
+    L = ctypes.CDLL(LIB_PATH)
+    _declare(L)
+    _lib = L
+    return L
+
+
+_P = ctypes.c_void_p
+_U32 = ctypes.c_uint32
+_U64 = ctypes.c_uint64
+_I = ctypes.c_int
+
+# name -> argtypes; every function returns int (bi_status) unless listed in _RESTYPE
+SIGNATURES: dict[str, list] = {
+    "bi_add_u64": [_P, _P, _P, _U32, _U64, _P],
+    "bi_add_u32": [_P, _P, _P, _U32, _U64, _P],
+    "bi_sub_u64": [_P, _P, _P, _P, _U32, _U64, _P],
+    "bi_sub_u32": [_P, _P, _P, _P, _U32, _U64, _P],
+    "bi_host_add_u64": [_P, _P, _P, _U32, _U64],
+    "bi_host_add_u32": [_P, _P, _P, _U32, _U64],
+    "bi_host_sub_u64": [_P, _P, _P, _P, _U32, _U64],
+    "bi_host_sub_u32": [_P, _P, _P, _P, _U32, _U64],
+    "bi_status_string": [_I],
+    "bi_last_error": [],
+    "bi_version": [],
+    "bi_max_limbs_addsub_u64": [],
+    "bi_max_limbs_addsub_u32": [],
+    "bi_fill_splitmix64": [_P, _U64, _U64, _U64, _P],
+    "bi_probe_intpipe": [_P, _P],
+}
+_RESTYPE = {
+    "bi_status_string": ctypes.c_char_p,
+    "bi_last_error": ctypes.c_char_p,
+    "bi_max_limbs_addsub_u64": _U32,
+    "bi_max_limbs_addsub_u32": _U32,
+}
+
+
+def _declare(L: ctypes.CDLL) -> None:
+    for name, args in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = _RESTYPE.get(name, _I)
+
+
+def _check(status: int) -> None:
+    if status != 0:
+        detail = lib().bi_last_error().decode(errors="replace")
+        raise BigIntError(status, detail)
+
+
+# ---------------------------------------------------------------------------
+# device-tensor helpers
+# ---------------------------------------------------------------------------
+
+def _wsuffix(t) -> str:
+    size = t.element_size()
+    if size == 8:
+        return "u64"
+    if size == 4:
+        return "u32"
+    raise TypeError("limb tensors must have 4- or 8-byte elements")
+
+
+def _stream_ptr(stream) -> int:
+    import torch
+
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return int(stream.cuda_stream)
+
+
+def _dev2d(t, name: str):
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if t.dim() != 2 or not t.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous [n, m] tensor")
+    return t
+
+
+def add(a, b, out=None, stream=None):
+    """r = (a + b) mod B^m per row."""
+    import torch
+
+    _dev2d(a, "a"), _dev2d(b, "b")
+    n, m = a.shape
+    if out is None:
+        out = torch.empty_like(a)
+    w = _wsuffix(a)
+    _check(getattr(lib(), f"bi_add_{w}")(a.data_ptr(), b.data_ptr(), out.data_ptr(), m, n, _stream_ptr(stream)))
+    return out
+
+
+def sub(a, b, out=None, sign=None, stream=None):
+    """(|a - b|, sign) per row; sign[i] = 1 where a_i < b_i."""
+    import torch
+
+    _dev2d(a, "a"), _dev2d(b, "b")
+    n, m = a.shape
+    if out is None:
+        out = torch.empty_like(a)
+    if sign is None:
+        sign = torch.empty(n, dtype=torch.uint8, device=a.device)
+    w = _wsuffix(a)
+    _check(getattr(lib(), f"bi_sub_{w}")(a.data_ptr(), b.data_ptr(), out.data_ptr(), sign.data_ptr(),
+                                         m, n, _stream_ptr(stream)))
+    return out, sign
+
+
+def fill_splitmix64(t, seed: int, offset: int = 0, stream=None):
+    """Fill an 8-byte-element CUDA tensor with the splitmix64 stream ``seed``."""
+    if not t.is_cuda or t.element_size() != 8 or not t.is_contiguous():
+        raise ValueError("fill_splitmix64 needs a contiguous CUDA tensor of 8-byte elements")
+    _check(lib().bi_fill_splitmix64(t.data_ptr(), t.numel(), seed & (2**64 - 1), offset, _stream_ptr(stream)))
+    return t
+
+
+PROBE_FORMS = ("mad.lo.u32", "mad.hi.u32", "mad.wide.u32", "mad.cc carry-chain rows", "mul.lo/hi.u64")
+
+
+def probe_intpipe(stream=None) -> dict:
+    """Measured 32x32-bit word products per second for each instruction form."""
+    rates = (ctypes.c_double * 5)()
+    _check(lib().bi_probe_intpipe(ctypes.cast(rates, ctypes.c_void_p), _stream_ptr(stream)))
+    return dict(zip(PROBE_FORMS, list(rates)))
+
+
+# ---------------------------------------------------------------------------
+# host (numpy) entry points: the reference's synchronous wrapper shape
+# ---------------------------------------------------------------------------
+
+def _np_w(a: np.ndarray) -> str:
+    if a.dtype == np.uint64:
+        return "u64"
+    if a.dtype == np.uint32:
+        return "u32"
+    raise TypeError("limb arrays must be uint32 or uint64")
+
+
+def _nptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def host_add(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    n, m = a.shape
+    r = np.empty_like(a)
+    _check(getattr(lib(), f"bi_host_add_{_np_w(a)}")(_nptr(a), _nptr(b), _nptr(r), m, n))
+    return r
+
+
+def host_sub(a: np.ndarray, b: np.ndarray):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    n, m = a.shape
+    r = np.empty_like(a)
+    s = np.empty(n, dtype=np.uint8)
+    _check(getattr(lib(), f"bi_host_sub_{_np_w(a)}")(_nptr(a), _nptr(b), _nptr(r), _nptr(s), m, n))
+    return r, s
+
+
+# ---------------------------------------------------------------------------
+# numpy <-> torch bit-preserving transfers (torch has no full uint64 support)
+# ---------------------------------------------------------------------------
+
+def to_device(x: np.ndarray, device="cuda"):
+    import torch
+
+    x = np.ascontiguousarray(x)
+    view = {8: np.int64, 4: np.int32, 1: np.uint8}[x.dtype.itemsize]
+    return torch.from_numpy(x.view(view)).to(device)
+
+
+def to_host(t, dtype) -> np.ndarray:
+    return t.cpu().numpy().view(dtype)

@@ -1,0 +1,146 @@
+"""Seeded synthetic inputs with the shapes of the benchmarked workloads.
+
+The reference benchmarks on unseeded ``rand()`` digits (cuda/helpers.h:96-111);
+here every input comes from a splitmix64 stream so runs are reproducible on
+any machine.  Seeds are 1000 + the workload index:
+
+  * mul2048_u32  -- 4096 pairs of 64-limb u32 integers (2048 bits), 10 % of
+                    pairs all-0xFFFFFFFF; full 128-limb product.
+  * addsub_u64   -- u64 limbs, sizes 2^10..2^18 bits, n = 2^27 / m instances;
+                    80 % uniform, 20 % carry-chain instances (add: a low run
+                    of all-ones limbs of length L in [m/2, m], b's low limb
+                    odd; sub: a low run of zero limbs, b = 1).
+  * mul_u64      -- u64 limbs, m in {64, 256, 1024, 2048}, n in
+                    {2^16, 2^14, 2^12, 2^11}, uniform; full 2m-limb product.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+GAMMA = np.uint64(0x9E3779B97F4A7C15)
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+
+
+def splitmix64(seed: int, count: int, offset: int = 0) -> np.ndarray:
+    """``count`` outputs of the splitmix64 stream ``seed``, starting at ``offset``."""
+    with np.errstate(over="ignore"):
+        idx = np.arange(offset + 1, offset + count + 1, dtype=np.uint64)
+        z = np.uint64(seed) + idx * GAMMA
+        z = (z ^ (z >> np.uint64(30))) * _M1
+        z = (z ^ (z >> np.uint64(27))) * _M2
+        return z ^ (z >> np.uint64(31))
+
+
+def uniform_limbs(seed: int, n: int, m: int, dtype=np.uint64, offset: int = 0) -> np.ndarray:
+    if dtype == np.uint64:
+        return splitmix64(seed, n * m, offset).reshape(n, m)
+    if dtype == np.uint32:
+        w = splitmix64(seed, (n * m + 1) // 2, offset).view(np.uint32)[: n * m]
+        return w.reshape(n, m).copy()
+    raise TypeError(dtype)
+
+
+def pick(seed: int, n: int, frac: float) -> np.ndarray:
+    """Boolean mask selecting about ``frac`` of ``n`` instances."""
+    u = splitmix64(seed ^ 0x5EED, n) >> np.uint64(11)
+    return (u.astype(np.float64) * (1.0 / (1 << 53))) < frac
+
+
+# ---------------------------------------------------------------------------
+
+def mul2048_u32(seed: int = 1000, n: int = 4096, m: int = 64):
+    a = uniform_limbs(seed, n, m, np.uint32)
+    b = uniform_limbs(seed, n, m, np.uint32, offset=(n * m + 1) // 2)
+    ones = pick(seed, n, 0.10)
+    a[ones] = 0xFFFFFFFF
+    b[ones] = 0xFFFFFFFF
+    return a, b
+
+
+ADDSUB_BITS = [1 << k for k in range(10, 19)]   # 2^10 .. 2^18 bits
+
+
+def _chains(bits: int, seed: int, n: int, m: int):
+    """Indices of the carry-chain instances and their run lengths in [m/2, m]."""
+    chain = np.nonzero(pick(seed + bits, n, 0.20))[0]
+    lens = m // 2 + (splitmix64(seed + 7 * bits, chain.size) % np.uint64(m - m // 2 + 1)).astype(np.int64)
+    return chain, lens
+
+
+def addsub_u64(bits: int, seed: int = 1001, total_limbs: int = 1 << 27, op: str = "add"):
+    """Inputs for one size of the add/sub sweep (u64 limbs, n*m = total_limbs)."""
+    m = bits // 64
+    n = total_limbs // m
+    a = uniform_limbs(seed, n, m)
+    b = uniform_limbs(seed, n, m, offset=n * m)
+    chain, lens = _chains(bits, seed, n, m)
+    if chain.size:
+        cols = np.arange(m)[None, :]
+        run = cols < lens[:, None]
+        if op == "add":
+            rows = a[chain]
+            rows[run] = np.uint64(0xFFFFFFFFFFFFFFFF)
+            a[chain] = rows
+            b[chain, 0] |= np.uint64(1)
+        else:
+            rows = a[chain]
+            rows[run] = np.uint64(0)
+            a[chain] = rows
+            b[chain] = 0
+            b[chain, 0] = 1
+    return a, b
+
+
+MUL_U64 = [(64, 1 << 16), (256, 1 << 14), (1024, 1 << 12), (2048, 1 << 11)]
+
+
+def mul_u64(m: int, n: int, seed: int = 1002):
+    a = uniform_limbs(seed, n, m)
+    b = uniform_limbs(seed, n, m, offset=n * m)
+    return a, b
+
+
+# ---------------------------------------------------------------------------
+# Device-side generation (same values as above, built on the GPU with the
+# library's splitmix64 fill kernel; tensors are int64 holding u64 limb bits)
+# ---------------------------------------------------------------------------
+
+def device_uniform_u64(seed: int, n: int, m: int, offset: int = 0, device="cuda"):
+    import torch
+
+    from . import fill_splitmix64
+
+    t = torch.empty((n, m), dtype=torch.int64, device=device)
+    fill_splitmix64(t, seed, offset)
+    return t
+
+
+def addsub_u64_device(bits: int, seed: int = 1001, total_limbs: int = 1 << 27, op: str = "add",
+                      device="cuda"):
+    import torch
+
+    m = bits // 64
+    n = total_limbs // m
+    a = device_uniform_u64(seed, n, m, device=device)
+    b = device_uniform_u64(seed, n, m, offset=n * m, device=device)
+    chain, lens = _chains(bits, seed, n, m)
+    if chain.size:
+        ci = torch.from_numpy(chain).to(device)
+        run = torch.arange(m, device=device)[None, :] < torch.from_numpy(lens).to(device)[:, None]
+        rows = a[ci]
+        if op == "add":
+            rows[run] = -1
+            a[ci] = rows
+            b[ci, 0] |= 1
+        else:
+            rows[run] = 0
+            a[ci] = rows
+            b[ci] = 0
+            b[ci, 0] = 1
+    return a, b
+
+
+def mul_u64_device(m: int, n: int, seed: int = 1002, device="cuda"):
+    return (device_uniform_u64(seed, n, m, device=device),
+            device_uniform_u64(seed, n, m, offset=n * m, device=device))

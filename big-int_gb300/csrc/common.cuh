@@ -1,0 +1,109 @@
+// common.cuh -- shared device and host helpers of the GB300 big-integer library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bigint_gb300.h"
+
+namespace bi {
+
+// ---------------------------------------------------------------------------
+// Limb traits.  The reference's U32bits/U64bits (cuda/ker-helpers.cu.h:28-44)
+// carry a 2-word type for products; here products are formed with explicit
+// mul.hi/mad instructions, so only the word type and its all-ones value are
+// needed.
+// ---------------------------------------------------------------------------
+template <typename T> struct Limb;
+template <> struct Limb<uint32_t> {
+    static constexpr uint32_t HIGHEST = 0xFFFFFFFFu;
+    static constexpr int BITS = 32;
+};
+template <> struct Limb<uint64_t> {
+    static constexpr uint64_t HIGHEST = 0xFFFFFFFFFFFFFFFFull;
+    static constexpr int BITS = 64;
+};
+
+// ---------------------------------------------------------------------------
+// Division by a runtime constant (Granlund-Montgomery, round-up variant).
+// Exact for every 32-bit numerator and divisor >= 1.
+// ---------------------------------------------------------------------------
+struct FastDiv {
+    uint32_t d;
+    uint32_t magic;
+    uint32_t shift;
+
+    __host__ __device__ FastDiv() : d(1), magic(0), shift(0) {}
+    __host__ explicit FastDiv(uint32_t divisor) : d(divisor) {
+        uint32_t l = 0;
+        while (l < 32 && (1ull << l) < divisor) l++;
+        shift = l;
+        // magic = floor(2^32 * (2^l - d) / d) + 1
+        magic = (uint32_t)((((1ull << l) - divisor) << 32) / divisor + 1);
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t x) const {
+        uint64_t t = __umulhi(x, magic);
+        return (uint32_t)((t + x) >> shift);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Carry lookahead across the 32 lanes of a warp.
+//
+// The reference propagates a 2-bit carry class (bit0 = generates a carry,
+// bit1 = propagates one) with an associative operator and a shared-memory
+// block scan (CarryProp/SegCarryProp, cuda/ker-add.cu.h:10-41; scanIncBlock,
+// cuda/ker-helpers.cu.h:66-95).  Here the classes of the 32 lanes are packed
+// into two 32-bit ballots and resolved by one integer addition: with
+// A = generate|propagate and B = generate, the carry out of bit t of A + B is
+// exactly g_t | (p_t & c_t).  The carry into each lane is therefore bit t of
+// (A + B + cin) ^ A ^ B, and bit 32 of the 64-bit sum is the carry out of
+// lane 31.  A lane whose successor starts a new instance has its classes
+// cleared so no carry crosses the instance boundary (the segment flag of
+// SegCarryProp).
+// ---------------------------------------------------------------------------
+struct WarpCarry {
+    uint32_t carries;   // bit t: carry into lane t
+    uint32_t cout;      // carry out of lane 31
+};
+
+__device__ __forceinline__ WarpCarry warp_carry_resolve(uint32_t A, uint32_t B, uint32_t cin) {
+    uint64_t s = (uint64_t)A + (uint64_t)B + (uint64_t)cin;
+    WarpCarry w;
+    w.carries = (uint32_t)s ^ A ^ B;
+    w.cout = (uint32_t)(s >> 32);
+    return w;
+}
+
+__device__ __forceinline__ uint32_t lane_id() {
+    uint32_t l;
+    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+    return l;
+}
+
+// ---------------------------------------------------------------------------
+// Streaming 16-byte global loads and stores (each limb is touched once).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 ld_stream16(const void* p) {
+    uint4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.L2::evict_first.v4.u32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ void st_stream16(void* p, uint4 v) {
+    asm volatile("st.global.cs.v4.u32 [%0], {%1,%2,%3,%4};"
+                 :: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
+}
+
+}  // namespace bi
+
+// ---------------------------------------------------------------------------
+// Host-side status plumbing (defined in capi.cu).
+// ---------------------------------------------------------------------------
+namespace bi {
+bi_status set_error(bi_status st, const char* fmt, ...);
+bi_status check_launch(const char* what);
+int num_sms();
+}  // namespace bi

@@ -1,0 +1,117 @@
+/*
+ * bigint_gb300.h -- C ABI of the GB300 batched big-integer library.
+ *
+ * Batches are flat row-major arrays [n][m] of little-endian limbs (u32 or
+ * u64): instance i occupies limbs [i*m, (i+1)*m), least significant limb
+ * first.  This is the layout of the reference's kernels and host wrappers
+ * (tossenxD/big-int cuda/ker-helpers.cu.h:117-187, cuda/main.cu:118-128).
+ *
+ * Conventions (replacing the reference's print-and-continue gpuAssert and
+ * exit()-ing CUDA_CHECK, cuda/helpers.h:21-27,192-203):
+ *   - every call returns a bi_status; BI_OK is 0; no call ever exits;
+ *   - device entry points take device pointers and a CUDA stream (a
+ *     cudaStream_t passed as bi_stream; NULL means the legacy default
+ *     stream); they are asynchronous with respect to the host and
+ *     stream-ordered, and they allocate no memory;
+ *   - host entry points (bi_host_*) take host pointers, allocate device
+ *     buffers, copy, launch, copy back and free, synchronously -- the shape
+ *     of the reference's gpuAdd/gpuMultiply wrappers;
+ *   - n == 0 is a no-op; m == 0 or a NULL buffer with n > 0 is BI_EINVAL;
+ *   - any n is accepted: unlike the reference launch (grid = n/ipb, which
+ *     drops the remainder, cuda/main.cu:135,307) every instance is computed;
+ *   - device buffers need the natural alignment of their limb type; 16-byte
+ *     aligned buffers take the vectorised path;
+ *   - calls are thread-safe; concurrent calls on different streams overlap.
+ */
+#ifndef BIGINT_GB300_H
+#define BIGINT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int bi_status;
+#define BI_OK            0
+#define BI_EINVAL        1  /* bad size, NULL pointer, misaligned buffer */
+#define BI_EDIV0         2  /* a divisor was zero (host division entry) */
+#define BI_ENOMEM        3  /* device allocation failed (host entries) */
+#define BI_ETIMEDOUT     4  /* a bounded device wait gave up */
+#define BI_ECUDA         5  /* a CUDA runtime call or launch failed */
+#define BI_EUNSUPPORTED  6  /* size beyond what this build supports */
+
+typedef void* bi_stream;
+
+/* Human-readable name of a status code. */
+const char* bi_status_string(bi_status status);
+
+/* Detail text of the last failing call on the calling thread ("" if none). */
+const char* bi_last_error(void);
+
+/* Library version as 10000*major + 100*minor + patch. */
+int bi_version(void);
+
+/* Largest m (in limbs) the one-instance-per-tile add/sub kernels accept. */
+uint32_t bi_max_limbs_addsub_u64(void);
+uint32_t bi_max_limbs_addsub_u32(void);
+
+/* ---------------------------------------------------------------------- */
+/* Addition: r_i = (a_i + b_i) mod B^m, carry-out dropped.                 */
+/* Replaces baddKer1/2/3 (cuda/ker-add.cu.h:69-86, 152-172, 246-266) as    */
+/* launched by gpuAdd (cuda/main.cu:108-222).  r may alias a or b.         */
+/* ---------------------------------------------------------------------- */
+bi_status bi_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                     uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                     uint32_t m, uint64_t n, bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
+/* Signed (sign-magnitude) subtraction: r_i = |a_i - b_i|,                 */
+/* sign[i] = 1 if a_i < b_i else 0.  Replaces bsub (futhark/sub.fut:14-26),*/
+/* exported there as test_sub (futhark/test/gmp-validation-lib.fut:16-17), */
+/* which the reference validates against mpz_abs(a - b)                    */
+/* (futhark/test/gmp-validation.c:38-41).  sign may be NULL.               */
+/* ---------------------------------------------------------------------- */
+bi_status bi_sub_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                     uint8_t* sign, uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                     uint8_t* sign, uint32_t m, uint64_t n, bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
+/* Host-pointer twins of the above (synchronous; allocate per call).       */
+/* Mirror gpuAdd<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:108-110).    */
+/* ---------------------------------------------------------------------- */
+bi_status bi_host_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                          uint32_t m, uint64_t n);
+bi_status bi_host_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                          uint32_t m, uint64_t n);
+bi_status bi_host_sub_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                          uint8_t* sign, uint32_t m, uint64_t n);
+bi_status bi_host_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                          uint8_t* sign, uint32_t m, uint64_t n);
+
+/* ---------------------------------------------------------------------- */
+/* Synthetic inputs: dst[i] = splitmix64 output number offset+i+1 of the   */
+/* stream `seed`.  No counterpart in the reference, whose benchmarks draw  */
+/* unseeded rand() digits (cuda/helpers.h:96-111); this makes multi-GiB    */
+/* benchmark inputs reproducible and cheap to create on the device.        */
+/* ---------------------------------------------------------------------- */
+bi_status bi_fill_splitmix64(uint64_t* dst, uint64_t count, uint64_t seed,
+                             uint64_t offset, bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
+/* Integer-pipe probe: rates[0..4] = 32x32-bit word products per second    */
+/* the GPU sustains with (0) mad.lo.u32, (1) mad.hi.u32, (2) mad.wide.u32, */
+/* (3) mad.lo.cc/madc.hi.cc carry-chain rows, (4) mul.lo/hi.u64.  The      */
+/* multiply roofline's denominator; no counterpart in the reference.       */
+/* Synchronous on `stream`.                                                */
+/* ---------------------------------------------------------------------- */
+bi_status bi_probe_intpipe(double* rates, bi_stream stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BIGINT_GB300_H */

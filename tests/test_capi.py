@@ -1,0 +1,76 @@
+"""CPU tests of the C ABI boundary: the library builds for sm_103a, loads,
+exports every function include/*.h declares, and validates arguments before
+it touches a GPU (no compute call is made here)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for mt in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(bi_\w+)\s*\(", src, flags=re.M):
+            names.add(mt.group(1))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def L():
+    import bigint_gb300 as B
+
+    B.build()
+    return B.lib()
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("bi_add_u64", "bi_sub_u64", "bi_host_add_u64", "bi_status_string"):
+        assert must in names
+
+
+def test_every_declared_symbol_is_exported(L):
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_python_signatures_cover_header(L):
+    import bigint_gb300 as B
+
+    missing = [n for n in declared_functions() if n not in B.SIGNATURES]
+    assert not missing, missing
+
+
+def test_status_strings(L):
+    assert L.bi_status_string(0) == b"BI_OK"
+    assert L.bi_status_string(2) == b"BI_EDIV0"
+    assert L.bi_version() >= 100
+
+
+def test_zero_instances_is_noop(L):
+    p = ctypes.c_void_p(0)
+    assert L.bi_add_u64(p, p, p, 4, 0, None) == 0
+    assert L.bi_sub_u32(p, p, p, p, 4, 0, None) == 0
+
+
+def test_invalid_arguments_rejected_before_launch(L):
+    fake = ctypes.c_void_p(0x1000)          # never dereferenced: validation fails first
+    assert L.bi_add_u64(fake, fake, fake, 0, 5, None) == 1          # m == 0
+    assert L.bi_add_u64(None, fake, fake, 4, 5, None) == 1         # NULL
+    assert L.bi_add_u64(ctypes.c_void_p(0x1004), fake, fake, 4, 5, None) == 1  # misaligned
+    assert b"aligned" in L.bi_last_error()
+    big = L.bi_max_limbs_addsub_u64() + 2
+    assert L.bi_add_u64(fake, fake, fake, big, 1, None) == 6         # unsupported size
+
+
+def test_library_built_for_sm103a():
+    import bigint_gb300 as B
+
+    assert "arch=compute_103a,code=sm_103a" in " ".join(B._build.ARCH)
+    assert os.path.exists(B.LIB_PATH)

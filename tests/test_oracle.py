@@ -1,0 +1,99 @@
+"""CPU tests: the oracle against the golden fixtures, the reference's KATs,
+Python integers, and (where it was built) the reference's own div.c."""
+import numpy as np
+import pytest
+
+from conftest import limbs
+from bigint_gb300.workloads import splitmix64
+
+
+def _int(row):
+    bits = row.dtype.itemsize * 8
+    return sum(int(x) << (bits * i) for i, x in enumerate(row))
+
+
+def test_little_endian(oracle):
+    assert oracle.lib().orc_little_endian() == 1
+
+
+def test_golden_arith(oracle, golden):
+    for c in golden["arith"]:
+        a, b = limbs(c["a"], c["bits"]), limbs(c["b"], c["bits"])
+        assert (oracle.add(a, b) == limbs(c["add"], c["bits"])).all()
+        r, s = oracle.sub(a, b)
+        assert (r == limbs(c["sub"], c["bits"])).all()
+        assert (s == np.array(c["sign"], np.uint8)).all()
+        assert (oracle.mul(a, b) == limbs(c["mul"], c["bits"])).all()
+        assert (oracle.mulfull(a, b) == limbs(c["mulfull"], c["bits"])).all()
+
+
+def test_golden_div(oracle, golden):
+    for c in golden["div"]:
+        u, v = limbs(c["u"], c["bits"]), limbs(c["v"], c["bits"])
+        q, r, st = oracle.div(u, v)
+        assert (st == 0).all()
+        assert (q == limbs(c["q"], c["bits"])).all(), (c["bits"], c["mu"], c["mv"])
+        assert (r == limbs(c["r"], c["bits"])).all(), (c["bits"], c["mu"], c["mv"])
+
+
+def test_reference_kats(oracle, golden):
+    for k in golden["kat"]:
+        u, v = limbs([k["u"]], 32), limbs([k["v"]], 32)
+        q, r, _ = oracle.div(u, v)
+        assert [int(x) for x in q[0]] == k["q"], k["source"]
+        assert [int(x) for x in r[0]] == k["r"], k["source"]
+
+
+def test_kat_values_stated_by_reference():
+    # futhark/div.fut:185-186 states the u16 quotient [5764, 41927, 1]
+    U = 33986 + (5952 << 16) + (61904 << 32)
+    assert U // 37752 == 5764 + (41927 << 16) + (1 << 32)
+
+
+@pytest.mark.parametrize("m", [2, 5, 16, 40])
+def test_div_matches_reference_div_c(oracle, m):
+    if oracle.ref_div_lib() is None:
+        pytest.skip("reference div.c not built here")
+    n = 3 * m
+    u = (splitmix64(11 + m, n * m) & np.uint64(0xFFFFFFFF)).astype(np.uint32).reshape(n, m)
+    v = (splitmix64(12 + m, n * m) & np.uint64(0xFFFFFFFF)).astype(np.uint32).reshape(n, m)
+    for i in range(n):                      # divisor precisions 1..m (div.c:509-523)
+        v[i, 1 + i % m:] = 0
+        v[i, 0] |= 1
+    q, r, _ = oracle.div(u, v)
+    qr, rr = oracle.ref_div_u32(u, v)
+    assert (q == qr).all() and (r == rr).all()
+
+
+def test_div_special_cases(oracle):
+    B = 1 << 32
+    cases = [
+        (B**4 - 1, 1), (B**4 - 1, B - 1), (B**3, B), (B**3, B**2), (B**3 + 5, B**2),
+        (B**4 - 1, B**3 + 1), (12345, 1 << 100), (B**4 - 1, (B**4 - 1) // 2 + 1),
+        (0, 7), (B**4 - 2, B**4 - 1), (B**4 - 1, B**4 - 1), (B**2 * 3, 2 * B + 1),
+    ]
+    m = 5
+    u = np.array([[(x >> (32 * i)) & (B - 1) for i in range(m)] for x, _ in cases], np.uint32)
+    v = np.array([[(y >> (32 * i)) & (B - 1) for i in range(m)] for _, y in cases], np.uint32)
+    q, r, _ = oracle.div(u, v)
+    for i, (x, y) in enumerate(cases):
+        assert _int(q[i]) == x // y and _int(r[i]) == x % y, (x, y)
+
+
+def test_div_by_zero_flagged(oracle):
+    u = np.ones((2, 4), np.uint64)
+    v = np.zeros((2, 2), np.uint64)
+    v[1, 0] = 3
+    q, r, st = oracle.div(u, v)
+    assert list(st) == [1, 0]
+    assert (q[0] == 0).all() and (r[0] == 0).all()
+
+
+def test_threaded_matches_single(oracle):
+    n, m = 64, 12
+    a = splitmix64(5, n * m).reshape(n, m)
+    b = splitmix64(6, n * m).reshape(n, m)
+    assert (oracle.mulfull(a, b, nthreads=4) == oracle.mulfull(a, b)).all()
+    r1, s1 = oracle.sub(a, b, nthreads=3)
+    r2, s2 = oracle.sub(a, b)
+    assert (r1 == r2).all() and (s1 == s2).all()
