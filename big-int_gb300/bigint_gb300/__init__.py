@@ -174,12 +174,13 @@ def fill_splitmix64(t, seed: int, offset: int = 0, stream=None):
     return t
 
 
-PROBE_FORMS = ("mad.lo.u32", "mad.hi.u32", "mad.wide.u32", "mad.cc carry-chain rows", "mul.lo/hi.u64")
+PROBE_FORMS = ("mad.lo.u32", "mad.hi.u32", "mad.wide.u32", "mad.cc carry-chain rows", "mul.lo/hi.u64",
+               "mad.wide.u32 column sums")
 
 
 def probe_intpipe(stream=None) -> dict:
     """Measured 32x32-bit word products per second for each instruction form."""
-    rates = (ctypes.c_double * 5)()
+    rates = (ctypes.c_double * 6)()
     _check(lib().bi_probe_intpipe(ctypes.cast(rates, ctypes.c_void_p), _stream_ptr(stream)))
     return dict(zip(PROBE_FORMS, list(rates)))
 

@@ -10,6 +10,8 @@
 //   2  mad.wide.u32 with 64-bit addend  (1 instruction  = 1 word product)
 //   3  row of mad.lo.cc / madc.hi.cc carry chains, 8 products + 2 addc
 //   4  64x64 products via mul.lo.u64 + mul.hi.u64 (= 4 word products)
+//   5  column accumulation: one new row multiplicand, 8 mad.wide.u32 into
+//      eight 64-bit column sums (1 instruction = 1 word product)
 #include "common.cuh"
 
 namespace bi {
@@ -25,11 +27,12 @@ __global__ void __launch_bounds__(256) intpipe_kernel(uint32_t* sink, uint32_t i
         uint32_t x[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) x[k] = a ^ k;
+        // x[k] is both a multiplicand and the addend, so nothing is loop-invariant
         for (uint32_t i = 0; i < iters; i++) {
 #pragma unroll
             for (int k = 0; k < 8; k++) {
-                if (MODE == 0) asm volatile("mad.lo.u32 %0, %1, %2, %0;" : "+r"(x[k]) : "r"(a), "r"(b[k]));
-                else           asm volatile("mad.hi.u32 %0, %1, %2, %0;" : "+r"(x[k]) : "r"(a), "r"(b[k]));
+                if (MODE == 0) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(x[k]) : "r"(b[k]), "r"(a));
+                else           asm volatile("mad.hi.u32 %0, %0, %1, %0;" : "+r"(x[k]) : "r"(b[k]));
             }
         }
 #pragma unroll
@@ -38,10 +41,13 @@ __global__ void __launch_bounds__(256) intpipe_kernel(uint32_t* sink, uint32_t i
         uint64_t y[8];
 #pragma unroll
         for (int k = 0; k < 8; k++) y[k] = a + k;
+        // the low half of each accumulator is the next multiplicand
         for (uint32_t i = 0; i < iters; i++) {
 #pragma unroll
-            for (int k = 0; k < 8; k++)
-                asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(y[k]) : "r"(a), "r"(b[k]));
+            for (int k = 0; k < 8; k++) {
+                const uint32_t lo = (uint32_t)y[k];
+                asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(y[k]) : "r"(lo), "r"(b[k]));
+            }
         }
 #pragma unroll
         for (int k = 0; k < 8; k++) acc ^= (uint32_t)y[k] ^ (uint32_t)(y[k] >> 32);
@@ -77,6 +83,19 @@ __global__ void __launch_bounds__(256) intpipe_kernel(uint32_t* sink, uint32_t i
         }
 #pragma unroll
         for (int k = 0; k < 10; k++) acc ^= r[k];
+    } else if (MODE == 5) {
+        uint64_t y[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) y[k] = a + k;
+        uint32_t ai = a;
+        for (uint32_t i = 0; i < iters; i++) {
+            ai += 0x9E3779B9u;   // a new row multiplicand each iteration (IADD, not the multiply pipe)
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(y[k]) : "r"(ai), "r"(b[k]));
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) acc ^= (uint32_t)y[k] ^ (uint32_t)(y[k] >> 32);
     } else {
         uint64_t lo[4], hi[4];
         uint64_t A = ((uint64_t)a << 32) | (a * 3u);
@@ -120,9 +139,9 @@ static bi_status time_mode(uint32_t* sink, int blocks, uint32_t iters, cudaStrea
 
 using namespace bi;
 
-// rates[k] = word products per second for probe form k (see the top of this file).
+// rates[k], k = 0..5: word products per second for probe form k (see the top of this file).
 extern "C" bi_status bi_probe_intpipe(double* rates, bi_stream s) {
-    if (!rates) return set_error(BI_EINVAL, "rates must point to 5 doubles");
+    if (!rates) return set_error(BI_EINVAL, "rates must point to 6 doubles");
     cudaStream_t st = (cudaStream_t)s;
     const int blocks = num_sms() * 8;
     uint32_t* sink = nullptr;
@@ -133,14 +152,15 @@ extern "C" bi_status bi_probe_intpipe(double* rates, bi_stream s) {
     float ms = 0;
     bi_status r = BI_OK;
     // word products per thread per iteration of each form
-    const double wp[5] = {8 * 0.5, 8 * 0.5, 8.0, 8.0, 4 * 4.0};
-    for (int mode = 0; mode < 5 && r == BI_OK; mode++) {
+    const double wp[6] = {8 * 0.5, 8 * 0.5, 8.0, 8.0, 4 * 4.0, 8.0};
+    for (int mode = 0; mode < 6 && r == BI_OK; mode++) {
         switch (mode) {
         case 0: r = time_mode<0>(sink, blocks, iters, st, &ms); break;
         case 1: r = time_mode<1>(sink, blocks, iters, st, &ms); break;
         case 2: r = time_mode<2>(sink, blocks, iters, st, &ms); break;
         case 3: r = time_mode<3>(sink, blocks, iters, st, &ms); break;
-        default: r = time_mode<4>(sink, blocks, iters, st, &ms); break;
+        case 4: r = time_mode<4>(sink, blocks, iters, st, &ms); break;
+        default: r = time_mode<5>(sink, blocks, iters, st, &ms); break;
         }
         rates[mode] = (r == BI_OK && ms > 0) ? threads * iters * wp[mode] / (ms * 1e-3) : 0.0;
     }

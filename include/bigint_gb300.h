@@ -102,9 +102,10 @@ bi_status bi_fill_splitmix64(uint64_t* dst, uint64_t count, uint64_t seed,
                              uint64_t offset, bi_stream stream);
 
 /* ---------------------------------------------------------------------- */
-/* Integer-pipe probe: rates[0..4] = 32x32-bit word products per second    */
+/* Integer-pipe probe: rates[0..5] = 32x32-bit word products per second    */
 /* the GPU sustains with (0) mad.lo.u32, (1) mad.hi.u32, (2) mad.wide.u32, */
-/* (3) mad.lo.cc/madc.hi.cc carry-chain rows, (4) mul.lo/hi.u64.  The      */
+/* (3) mad.lo.cc/madc.hi.cc carry-chain rows, (4) mul.lo/hi.u64, (5)       */
+/* mad.wide.u32 accumulating 64-bit column sums.  The                      */
 /* multiply roofline's denominator; no counterpart in the reference.       */
 /* Synchronous on `stream`.                                                */
 /* ---------------------------------------------------------------------- */
