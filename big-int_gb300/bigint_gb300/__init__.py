@@ -85,6 +85,16 @@ SIGNATURES: dict[str, list] = {
     "bi_max_limbs_addsub_u64": [],
     "bi_max_limbs_addsub_u32": [],
     "bi_fill_splitmix64": [_P, _U64, _U64, _U64, _P],
+    "bi_mul_u64": [_P, _P, _P, _U32, _U64, _P],
+    "bi_mul_u32": [_P, _P, _P, _U32, _U64, _P],
+    "bi_mulfull_u64": [_P, _P, _P, _U32, _U64, _P],
+    "bi_mulfull_u32": [_P, _P, _P, _U32, _U64, _P],
+    "bi_host_mul_u64": [_P, _P, _P, _U32, _U64],
+    "bi_host_mul_u32": [_P, _P, _P, _U32, _U64],
+    "bi_host_mulfull_u64": [_P, _P, _P, _U32, _U64],
+    "bi_host_mulfull_u32": [_P, _P, _P, _U32, _U64],
+    "bi_max_limbs_mul_u64": [],
+    "bi_max_limbs_mul_u32": [],
     "bi_probe_intpipe": [_P, _P],
 }
 _RESTYPE = {
@@ -92,6 +102,8 @@ _RESTYPE = {
     "bi_last_error": ctypes.c_char_p,
     "bi_max_limbs_addsub_u64": _U32,
     "bi_max_limbs_addsub_u32": _U32,
+    "bi_max_limbs_mul_u64": _U32,
+    "bi_max_limbs_mul_u32": _U32,
 }
 
 
@@ -166,6 +178,32 @@ def sub(a, b, out=None, sign=None, stream=None):
     return out, sign
 
 
+def mul(a, b, out=None, stream=None):
+    """r = (a * b) mod B^m per row (the reference's truncated product)."""
+    import torch
+
+    _dev2d(a, "a"), _dev2d(b, "b")
+    n, m = a.shape
+    if out is None:
+        out = torch.empty_like(a)
+    _check(getattr(lib(), f"bi_mul_{_wsuffix(a)}")(a.data_ptr(), b.data_ptr(), out.data_ptr(), m, n,
+                                                  _stream_ptr(stream)))
+    return out
+
+
+def mulfull(a, b, out=None, stream=None):
+    """Full product per row: [n, 2m]."""
+    import torch
+
+    _dev2d(a, "a"), _dev2d(b, "b")
+    n, m = a.shape
+    if out is None:
+        out = torch.empty((n, 2 * m), dtype=a.dtype, device=a.device)
+    _check(getattr(lib(), f"bi_mulfull_{_wsuffix(a)}")(a.data_ptr(), b.data_ptr(), out.data_ptr(), m, n,
+                                                      _stream_ptr(stream)))
+    return out
+
+
 def fill_splitmix64(t, seed: int, offset: int = 0, stream=None):
     """Fill an 8-byte-element CUDA tensor with the splitmix64 stream ``seed``."""
     if not t.is_cuda or t.element_size() != 8 or not t.is_contiguous():
@@ -206,6 +244,22 @@ def host_add(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     n, m = a.shape
     r = np.empty_like(a)
     _check(getattr(lib(), f"bi_host_add_{_np_w(a)}")(_nptr(a), _nptr(b), _nptr(r), m, n))
+    return r
+
+
+def host_mul(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    n, m = a.shape
+    r = np.empty_like(a)
+    _check(getattr(lib(), f"bi_host_mul_{_np_w(a)}")(_nptr(a), _nptr(b), _nptr(r), m, n))
+    return r
+
+
+def host_mulfull(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    n, m = a.shape
+    r = np.empty((n, 2 * m), dtype=a.dtype)
+    _check(getattr(lib(), f"bi_host_mulfull_{_np_w(a)}")(_nptr(a), _nptr(b), _nptr(r), m, n))
     return r
 
 

@@ -139,4 +139,29 @@ bi_status bi_host_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uin
         });
 }
 
+bi_status bi_host_mul_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n) {
+    return host_binary<uint64_t>(a, b, r, nullptr, m, n, m,
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*) {
+            return bi_mul_u64(da, db, dr, m, n, nullptr);
+        });
+}
+bi_status bi_host_mul_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n) {
+    return host_binary<uint32_t>(a, b, r, nullptr, m, n, m,
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*) {
+            return bi_mul_u32(da, db, dr, m, n, nullptr);
+        });
+}
+bi_status bi_host_mulfull_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n) {
+    return host_binary<uint64_t>(a, b, r, nullptr, m, n, 2 * (size_t)m,
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*) {
+            return bi_mulfull_u64(da, db, dr, m, n, nullptr);
+        });
+}
+bi_status bi_host_mulfull_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n) {
+    return host_binary<uint32_t>(a, b, r, nullptr, m, n, 2 * (size_t)m,
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*) {
+            return bi_mulfull_u32(da, db, dr, m, n, nullptr);
+        });
+}
+
 }  // extern "C"

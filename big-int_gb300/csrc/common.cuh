@@ -75,6 +75,38 @@ __device__ __forceinline__ WarpCarry warp_carry_resolve(uint32_t A, uint32_t B, 
     return w;
 }
 
+// Carry into each thread of a CTA for a segmented carry chain that runs over
+// the threads in index order.  Thread t supplies the (generate, propagate)
+// pair of its stage and `seg` = 1 if it begins a new segment (no carry
+// enters it).  Returns the carry into the thread's stage.  Every thread of
+// the CTA must call it (blockDim.x a multiple of 32, at most 32 warps);
+// `scratch` holds 3 * 32 words of shared memory.  Contains __syncthreads.
+__device__ __forceinline__ uint32_t block_carry_in(uint32_t g, uint32_t p, bool seg, uint32_t* scratch) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const uint32_t S = __ballot_sync(0xffffffffu, seg);
+    const uint32_t kill = S >> 1;
+    const uint32_t A = __ballot_sync(0xffffffffu, g | p) & ~kill;
+    const uint32_t B = __ballot_sync(0xffffffffu, g) & ~kill;
+    if (lane == 0) {
+        const uint32_t g0 = warp_carry_resolve(A, B, 0).cout;
+        const uint32_t g1 = warp_carry_resolve(A, B, 1).cout;
+        scratch[warp] = g0;
+        scratch[32 + warp] = g1 & ~g0;
+        scratch[64 + warp] = S & 1u;
+    }
+    __syncthreads();
+    const bool before = lane < warp;
+    const bool killed = before && scratch[64 + (lane + 1 < nwarps ? lane + 1 : 0)];
+    const bool live = before && !killed;
+    const uint32_t wg = live ? scratch[lane] : 0u, wp = live ? scratch[32 + lane] : 0u;
+    const uint32_t A2 = __ballot_sync(0xffffffffu, wg | wp);
+    const uint32_t B2 = __ballot_sync(0xffffffffu, wg);
+    uint32_t cin = (warp_carry_resolve(A2, B2, 0).carries >> warp) & 1u;
+    if (S & 1u) cin = 0;
+    __syncthreads();   // scratch may be reused by the caller
+    return (warp_carry_resolve(A, B, cin).carries >> lane) & 1u;
+}
+
 __device__ __forceinline__ uint32_t lane_id() {
     uint32_t l;
     asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));

@@ -80,9 +80,39 @@ bi_status bi_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
                      uint8_t* sign, uint32_t m, uint64_t n, bi_stream stream);
 
 /* ---------------------------------------------------------------------- */
-/* Host-pointer twins of the above (synchronous; allocate per call).       */
-/* Mirror gpuAdd<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:108-110).    */
+/* Classical (quadratic) multiplication.                                   */
+/* bi_mul_*:     r_i = (a_i * b_i) mod B^m, r is [n][m] -- the truncated   */
+/*               product of convMul1..5 (cuda/ker-mul.cu.h:202-221,        */
+/*               310-329, 420-439, 532-551, 647-666) as launched by        */
+/*               gpuMultiply (cuda/main.cu:280-419).                       */
+/* bi_mulfull_*: r_i = a_i * b_i, r is [n][2m] -- the full product, which  */
+/*               the reference obtains only by zero-padding to 2m limbs.   */
+/* r must not overlap a or b.  m <= bi_max_limbs_mul_* ().                 */
 /* ---------------------------------------------------------------------- */
+uint32_t bi_max_limbs_mul_u64(void);
+uint32_t bi_max_limbs_mul_u32(void);
+bi_status bi_mul_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                     uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_mul_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                     uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_mulfull_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                         uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_mulfull_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                         uint32_t m, uint64_t n, bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
+/* Host-pointer twins of the above (synchronous; allocate per call).       */
+/* Mirror gpuAdd<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:108-110) and */
+/* gpuMultiply<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:280-282).      */
+/* ---------------------------------------------------------------------- */
+bi_status bi_host_mul_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                          uint32_t m, uint64_t n);
+bi_status bi_host_mul_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                          uint32_t m, uint64_t n);
+bi_status bi_host_mulfull_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                              uint32_t m, uint64_t n);
+bi_status bi_host_mulfull_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                              uint32_t m, uint64_t n);
 bi_status bi_host_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
                           uint32_t m, uint64_t n);
 bi_status bi_host_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
