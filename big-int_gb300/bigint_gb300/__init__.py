@@ -95,6 +95,12 @@ SIGNATURES: dict[str, list] = {
     "bi_host_mulfull_u32": [_P, _P, _P, _U32, _U64],
     "bi_max_limbs_mul_u64": [],
     "bi_max_limbs_mul_u32": [],
+    "bi_div_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
+    "bi_div_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
+    "bi_host_div_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64],
+    "bi_host_div_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64],
+    "bi_max_limbs_div_u64": [],
+    "bi_max_limbs_div_u32": [],
     "bi_probe_intpipe": [_P, _P],
 }
 _RESTYPE = {
@@ -104,6 +110,8 @@ _RESTYPE = {
     "bi_max_limbs_addsub_u32": _U32,
     "bi_max_limbs_mul_u64": _U32,
     "bi_max_limbs_mul_u32": _U32,
+    "bi_max_limbs_div_u64": _U32,
+    "bi_max_limbs_div_u32": _U32,
 }
 
 
@@ -204,6 +212,24 @@ def mulfull(a, b, out=None, stream=None):
     return out
 
 
+def div(u, v, q=None, r=None, status=None, stream=None):
+    """(q, r, status) per row: q = floor(u / v), r = u mod v; status 1 = zero divisor."""
+    import torch
+
+    _dev2d(u, "u"), _dev2d(v, "v")
+    n, mu = u.shape
+    mv = v.shape[1]
+    if q is None:
+        q = torch.empty_like(u)
+    if r is None:
+        r = torch.empty((n, mv), dtype=u.dtype, device=u.device)
+    if status is None:
+        status = torch.empty(n, dtype=torch.uint8, device=u.device)
+    _check(getattr(lib(), f"bi_div_{_wsuffix(u)}")(u.data_ptr(), v.data_ptr(), q.data_ptr(), r.data_ptr(),
+                                                  status.data_ptr(), mu, mv, n, _stream_ptr(stream)))
+    return q, r, status
+
+
 def fill_splitmix64(t, seed: int, offset: int = 0, stream=None):
     """Fill an 8-byte-element CUDA tensor with the splitmix64 stream ``seed``."""
     if not t.is_cuda or t.element_size() != 8 or not t.is_contiguous():
@@ -261,6 +287,18 @@ def host_mulfull(a: np.ndarray, b: np.ndarray) -> np.ndarray:
     r = np.empty((n, 2 * m), dtype=a.dtype)
     _check(getattr(lib(), f"bi_host_mulfull_{_np_w(a)}")(_nptr(a), _nptr(b), _nptr(r), m, n))
     return r
+
+
+def host_div(u: np.ndarray, v: np.ndarray):
+    """(q, r, status); raises BigIntError(BI_EDIV0) if any divisor is zero."""
+    u, v = np.ascontiguousarray(u), np.ascontiguousarray(v)
+    n, mu = u.shape
+    mv = v.shape[1]
+    q = np.empty_like(u)
+    r = np.empty((n, mv), dtype=u.dtype)
+    st = np.zeros(n, dtype=np.uint8)
+    _check(getattr(lib(), f"bi_host_div_{_np_w(u)}")(_nptr(u), _nptr(v), _nptr(q), _nptr(r), _nptr(st), mu, mv, n))
+    return q, r, st
 
 
 def host_sub(a: np.ndarray, b: np.ndarray):

@@ -6,6 +6,7 @@
 // report every failure as a status code instead of printing and carrying on.
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "common.cuh"
@@ -89,11 +90,60 @@ static bi_status host_binary(const T* ha, const T* hb, T* hr, uint8_t* hsign, ui
     return BI_OK;
 }
 
+template <typename T>
+static bi_status host_div(const T* hu, const T* hv, T* hq, T* hr, uint8_t* hstatus, uint32_t mu, uint32_t mv,
+                          uint64_t n) {
+    if (n == 0) return BI_OK;
+    if (mu == 0 || mv == 0 || mv > mu) return set_error(BI_EINVAL, "need 1 <= mv <= mu");
+    if (!hu || !hv || !hq || !hr) return set_error(BI_EINVAL, "NULL host buffer");
+    DevBuf du, dv, dq, dr, ds;
+    BI_TRY(du.alloc((size_t)n * mu * sizeof(T)));
+    BI_TRY(dv.alloc((size_t)n * mv * sizeof(T)));
+    BI_TRY(dq.alloc((size_t)n * mu * sizeof(T)));
+    BI_TRY(dr.alloc((size_t)n * mv * sizeof(T)));
+    BI_TRY(ds.alloc(n));
+    BI_TRY(cuda_ok(cudaMemcpy(du.p, hu, du.bytes, cudaMemcpyHostToDevice), "copy u"));
+    BI_TRY(cuda_ok(cudaMemcpy(dv.p, hv, dv.bytes, cudaMemcpyHostToDevice), "copy v"));
+    bi_status st;
+    if constexpr (sizeof(T) == 8)
+        st = bi_div_u64((const T*)du.p, (const T*)dv.p, (T*)dq.p, (T*)dr.p, (uint8_t*)ds.p, mu, mv, n, nullptr);
+    else
+        st = bi_div_u32((const T*)du.p, (const T*)dv.p, (T*)dq.p, (T*)dr.p, (uint8_t*)ds.p, mu, mv, n, nullptr);
+    BI_TRY(st);
+    BI_TRY(cuda_ok(cudaMemcpy(hq, dq.p, dq.bytes, cudaMemcpyDeviceToHost), "copy q"));
+    BI_TRY(cuda_ok(cudaMemcpy(hr, dr.p, dr.bytes, cudaMemcpyDeviceToHost), "copy r"));
+    uint8_t* stat = hstatus;
+    uint8_t* own = nullptr;
+    if (!stat) {
+        own = (uint8_t*)malloc(n);
+        if (!own) return set_error(BI_ENOMEM, "host status buffer");
+        stat = own;
+    }
+    bi_status rs = cuda_ok(cudaMemcpy(stat, ds.p, n, cudaMemcpyDeviceToHost), "copy status");
+    if (rs == BI_OK) {
+        for (uint64_t i = 0; i < n; i++) {
+            if (stat[i] == 1) { rs = set_error(BI_EDIV0, "instance %llu has a zero divisor", (unsigned long long)i); break; }
+            if (stat[i] == 2) { rs = set_error(BI_ECUDA, "instance %llu exceeded the correction bound", (unsigned long long)i); break; }
+        }
+    }
+    free(own);
+    return rs;
+}
+
 }  // namespace bi
 
 using namespace bi;
 
 extern "C" {
+
+bi_status bi_host_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r, uint8_t* status,
+                          uint32_t mu, uint32_t mv, uint64_t n) {
+    return host_div<uint64_t>(u, v, q, r, status, mu, mv, n);
+}
+bi_status bi_host_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r, uint8_t* status,
+                          uint32_t mu, uint32_t mv, uint64_t n) {
+    return host_div<uint32_t>(u, v, q, r, status, mu, mv, n);
+}
 
 const char* bi_status_string(bi_status s) {
     switch (s) {

@@ -26,7 +26,7 @@
 //   * The windows overlap by two limbs; a carry-lookahead across windows
 //     (block_carry_in) merges them, as the reference's final baddKer3Run
 //     merges its low/high/carry vectors (ker-mul.cu.h:588-645).
-#include "common.cuh"
+#include "blockops.cuh"   // row_mac8
 
 namespace bi {
 
@@ -34,36 +34,6 @@ namespace bi {
 template <int C>
 __device__ __forceinline__ uint32_t skew(uint32_t x) {
     return x + 2 * (x / C);
-}
-
-// R[0..C+2) += a * bw[0..C)  (bw given as ext[T0 .. T0+C))
-template <int T0>
-__device__ __forceinline__ void row_mac8(uint64_t (&R)[10], uint64_t a, const uint64_t (&e)[16]) {
-    asm volatile(
-        "{\n\t.reg .u64 t;\n\t"
-        "mul.lo.u64 t, %10, %11;\n\tadd.cc.u64  %0, %0, t;\n\t"
-        "mul.lo.u64 t, %10, %12;\n\taddc.cc.u64 %1, %1, t;\n\t"
-        "mul.lo.u64 t, %10, %13;\n\taddc.cc.u64 %2, %2, t;\n\t"
-        "mul.lo.u64 t, %10, %14;\n\taddc.cc.u64 %3, %3, t;\n\t"
-        "mul.lo.u64 t, %10, %15;\n\taddc.cc.u64 %4, %4, t;\n\t"
-        "mul.lo.u64 t, %10, %16;\n\taddc.cc.u64 %5, %5, t;\n\t"
-        "mul.lo.u64 t, %10, %17;\n\taddc.cc.u64 %6, %6, t;\n\t"
-        "mul.lo.u64 t, %10, %18;\n\taddc.cc.u64 %7, %7, t;\n\t"
-        "addc.cc.u64 %8, %8, 0;\n\t"
-        "addc.u64    %9, %9, 0;\n\t"
-        "mul.hi.u64 t, %10, %11;\n\tadd.cc.u64  %1, %1, t;\n\t"
-        "mul.hi.u64 t, %10, %12;\n\taddc.cc.u64 %2, %2, t;\n\t"
-        "mul.hi.u64 t, %10, %13;\n\taddc.cc.u64 %3, %3, t;\n\t"
-        "mul.hi.u64 t, %10, %14;\n\taddc.cc.u64 %4, %4, t;\n\t"
-        "mul.hi.u64 t, %10, %15;\n\taddc.cc.u64 %5, %5, t;\n\t"
-        "mul.hi.u64 t, %10, %16;\n\taddc.cc.u64 %6, %6, t;\n\t"
-        "mul.hi.u64 t, %10, %17;\n\taddc.cc.u64 %7, %7, t;\n\t"
-        "mul.hi.u64 t, %10, %18;\n\taddc.cc.u64 %8, %8, t;\n\t"
-        "addc.u64    %9, %9, 0;\n\t}"
-        : "+l"(R[0]), "+l"(R[1]), "+l"(R[2]), "+l"(R[3]), "+l"(R[4]), "+l"(R[5]), "+l"(R[6]),
-          "+l"(R[7]), "+l"(R[8]), "+l"(R[9])
-        : "l"(a), "l"(e[T0 + 0]), "l"(e[T0 + 1]), "l"(e[T0 + 2]), "l"(e[T0 + 3]), "l"(e[T0 + 4]),
-          "l"(e[T0 + 5]), "l"(e[T0 + 6]), "l"(e[T0 + 7]));
 }
 
 __device__ __forceinline__ void lds128(const uint64_t* p, uint64_t& x, uint64_t& y) {

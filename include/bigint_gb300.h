@@ -101,6 +101,28 @@ bi_status bi_mulfull_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
                          uint32_t m, uint64_t n, bi_stream stream);
 
 /* ---------------------------------------------------------------------- */
+/* Division with remainder: q_i = floor(u_i / v_i), r_i = u_i mod v_i.     */
+/* u is [n][mu], v is [n][mv] with mv <= mu, q is [n][mu], r is [n][mv].   */
+/* Replaces div_shinv (prototypes/div.c:427-467; quotient by a shifted     */
+/* inverse refined with shorter iterates and divisor prefixes) and the     */
+/* Futhark div / test_div (futhark/div.fut:150-167,                        */
+/* futhark/test/gmp-validation-lib.fut:26-27), which require equal sizes;  */
+/* here the divisor may be shorter.  status (may be NULL) is [n]:          */
+/* 0 = ok, 1 = divisor zero (q_i and r_i are set to 0), 2 = internal      */
+/* correction bound exceeded (never observed).  The reference divides by   */
+/* zero (div.c:165-181); this entry reports it per instance instead.       */
+/* mu <= bi_max_limbs_div_* ().                                            */
+/* ---------------------------------------------------------------------- */
+uint32_t bi_max_limbs_div_u64(void);
+uint32_t bi_max_limbs_div_u32(void);
+bi_status bi_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r,
+                     uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
+                     bi_stream stream);
+bi_status bi_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r,
+                     uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
+                     bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
 /* Host-pointer twins of the above (synchronous; allocate per call).       */
 /* Mirror gpuAdd<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:108-110) and */
 /* gpuMultiply<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:280-282).      */
@@ -113,6 +135,14 @@ bi_status bi_host_mulfull_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
                               uint32_t m, uint64_t n);
 bi_status bi_host_mulfull_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
                               uint32_t m, uint64_t n);
+/* Returns BI_EDIV0 (after computing every other instance) if any divisor  */
+/* was zero; status may be NULL.                                           */
+bi_status bi_host_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* q,
+                          uint64_t* r, uint8_t* status, uint32_t mu, uint32_t mv,
+                          uint64_t n);
+bi_status bi_host_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q,
+                          uint32_t* r, uint8_t* status, uint32_t mu, uint32_t mv,
+                          uint64_t n);
 bi_status bi_host_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
                           uint32_t m, uint64_t n);
 bi_status bi_host_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
