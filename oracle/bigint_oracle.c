@@ -294,9 +294,18 @@ static void shinv(dctx* c, const dg* v, int h, int k, dg* w) {
 }
 
 /* Quotient and remainder of u by v, both m digits, following div_shinv
- * (div.c:427-467): q = floor(u * shinv_h(v) / B^h) + delta, delta in {0,1}.
- * Internal precision is 4m digits as in the reference.  v must be nonzero. */
-static void div_one(const dg* u, const dg* v, dg* q, dg* r, uint32_t m) {
+ * (div.c:427-467): q = floor(u * shinv_h(v) / B^h) + delta.  Internal
+ * precision is 4m digits as in the reference.  v must be nonzero.
+ *
+ * `faithful` = 1 applies the reference's single delta step (delta in {0,1},
+ * div.c:459-463) exactly as written.  That step is not always enough: for
+ * some inputs the estimate is two short and div.c returns a remainder >= v
+ * (e.g. u = 0xdc4461359674c9cfd718dc1b567834b5, v = 0xdd2982a538271953 with
+ * m = 4 digits; about 0.05-0.4 % of random inputs whose divisor has half the
+ * dividend's digits).  `faithful` = 0 repeats the step while r >= v, which
+ * yields the exact quotient and remainder -- the results the reference
+ * itself validates against (mpz_div, div.c:470-486, 525-532). */
+static void div_one(const dg* u, const dg* v, dg* q, dg* r, uint32_t m, int faithful) {
     int p = 4 * (int)m;
     dg* buf = (dg*)calloc((size_t)p * 9, sizeof(dg));
     dg *a = buf, *b = buf + p, *cc = buf + 2 * p;
@@ -321,10 +330,11 @@ static void div_one(const dg* u, const dg* v, dg* q, dg* r, uint32_t m) {
     dg* vq = a;
     mul_into(v, m, q, m, vq, (uint32_t)p);
     (void)sub_one(u, vq, r, m);
-    if (!less_than(r, v, m)) {
+    while (!less_than(r, v, m)) {
         set_digit(a, 1, (int)m);
         add_one(q, a, q, m);
         (void)sub_one(r, v, r, m);
+        if (faithful) break;
     }
     free(buf);
 }
@@ -333,7 +343,7 @@ static void div_one(const dg* u, const dg* v, dg* q, dg* r, uint32_t m) {
 /* Batched entry points (u32 digits), optionally multi-threaded              */
 /* ------------------------------------------------------------------------ */
 
-enum { OP_ADD, OP_SUB, OP_MUL, OP_MULFULL, OP_DIV };
+enum { OP_ADD, OP_SUB, OP_MUL, OP_MULFULL, OP_DIV, OP_DIV_REF };
 
 typedef struct {
     int op;
@@ -361,7 +371,8 @@ static void run_range(job_t* j) {
         case OP_MULFULL:
             mul_into(j->a + i * m, m, j->b + i * m, m, j->r + 2 * i * m, 2 * m);
             break;
-        case OP_DIV: {
+        case OP_DIV:
+        case OP_DIV_REF: {
             /* dividend m digits, divisor mb <= m digits: pad the divisor to
              * m digits as the reference requires equal sizes (div.c:427) */
             uint32_t mb = j->mb;
@@ -380,7 +391,7 @@ static void run_range(job_t* j) {
             dg* vpad = (dg*)calloc(m, sizeof(dg));
             dg* rpad = (dg*)calloc(m, sizeof(dg));
             memcpy(vpad, vi, mb * sizeof(dg));
-            div_one(j->a + i * m, vpad, q, rpad, m);
+            div_one(j->a + i * m, vpad, q, rpad, m, j->op == OP_DIV_REF);
             memcpy(rr, rpad, mb * sizeof(dg));
             if (j->sign) j->sign[i] = 0;
             free(vpad);
@@ -441,6 +452,15 @@ int orc_div_u32(const dg* u, const dg* v, dg* q, dg* r, uint8_t* status,
                 uint32_t mu, uint32_t mv, uint64_t n, int nt) {
     if (mv > mu) return 1;
     job_t j = {OP_DIV, u, v, q, r, status, mu, mv, 0, 0, 0};
+    return run_batch(j, n, nt);
+}
+
+/* The reference's division exactly as written (single delta step); for
+ * pinning the oracle against prototypes/div.c and documenting its defect. */
+int orc_div_ref_u32(const dg* u, const dg* v, dg* q, dg* r, uint8_t* status,
+                    uint32_t mu, uint32_t mv, uint64_t n, int nt) {
+    if (mv > mu) return 1;
+    job_t j = {OP_DIV_REF, u, v, q, r, status, mu, mv, 0, 0, 0};
     return run_batch(j, n, nt);
 }
 

@@ -53,6 +53,8 @@ def lib():
             f = getattr(L, f"orc_div_{w}")
             f.argtypes = [P, P, P, P, P, U32, U32, U64, I]
             f.restype = I
+        L.orc_div_ref_u32.argtypes = [P, P, P, P, P, U32, U32, U64, I]
+        L.orc_div_ref_u32.restype = I
         L.orc_little_endian.restype = I
         if L.orc_little_endian() != 1:
             raise RuntimeError("oracle requires a little-endian host")
@@ -129,6 +131,20 @@ def div(u, v, nthreads: int = 1):
     r = np.empty((n, mv), dtype=u.dtype)
     st = np.zeros(n, dtype=np.uint8)
     getattr(lib(), f"orc_div_{_wname(u)}")(_p(u), _p(v), _p(q), _p(r), _p(st), mu, mv, n, nthreads)
+    return q, r, st
+
+
+def div_ref(u, v, nthreads: int = 1):
+    """The reference's division algorithm exactly as written (u32 digits,
+    single delta step, so occasionally one short -- see bigint_oracle.c)."""
+    u = _c(u).astype(np.uint32, copy=False)
+    v = _c(v).astype(np.uint32, copy=False)
+    n, mu = u.shape
+    mv = v.shape[1]
+    q = np.empty_like(u)
+    r = np.empty((n, mv), dtype=np.uint32)
+    st = np.zeros(n, dtype=np.uint8)
+    lib().orc_div_ref_u32(_p(u), _p(v), _p(q), _p(r), _p(st), mu, mv, n, nthreads)
     return q, r, st
 
 

@@ -119,3 +119,18 @@ def test_host_entry(bigint, oracle):
         q, r, st = B.host_div(u, v)
         q_ref, r_ref, _ = oracle.div(u, v)
         assert (q == q_ref).all() and (r == r_ref).all() and (st == 0).all()
+
+
+def test_exact_where_reference_prototype_is_one_short(bigint, oracle):
+    """prototypes/div.c returns q one short (r >= v) on this input; the GPU
+    division returns the exact quotient and remainder."""
+    U, V = 0xdc4461359674c9cfd718dc1b567834b5, 0xdd2982a538271953
+    u = np.array([[(U >> (32 * i)) & 0xFFFFFFFF for i in range(4)]], np.uint32)
+    v = np.array([[(V >> (32 * i)) & 0xFFFFFFFF for i in range(2)]], np.uint32)
+    q, r, st = bigint.div(bigint.to_device(u), bigint.to_device(v))
+    qv = bigint.to_host(q, np.uint32)[0]
+    rv = bigint.to_host(r, np.uint32)[0]
+    assert sum(int(x) << (32 * i) for i, x in enumerate(qv)) == U // V
+    assert sum(int(x) << (32 * i) for i, x in enumerate(rv)) == U % V
+    qf, _, _ = oracle.div_ref(u, np.array([[*v[0], 0, 0]], np.uint32))
+    assert sum(int(x) << (32 * i) for i, x in enumerate(qf[0])) == U // V - 1

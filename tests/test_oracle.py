@@ -97,3 +97,56 @@ def test_threaded_matches_single(oracle):
     r1, s1 = oracle.sub(a, b, nthreads=3)
     r2, s2 = oracle.sub(a, b)
     assert (r1 == r2).all() and (s1 == s2).all()
+
+
+# A documented defect of the reference's division prototype: its single
+# delta step (prototypes/div.c:459-463) leaves q one short for some inputs.
+REF_DIV_DEFECT = (0xdc4461359674c9cfd718dc1b567834b5, 0xdd2982a538271953, 4)
+
+
+def _digits(x, m):
+    return [(x >> (32 * i)) & 0xFFFFFFFF for i in range(m)]
+
+
+def test_faithful_restatement_matches_reference_div_c(oracle):
+    """div_ref is div.c as written: identical outputs, defect included."""
+    if oracle.ref_div_lib() is None:
+        pytest.skip("reference div.c not built here")
+    for m in (3, 4, 5, 8, 16):
+        n = 600
+        u = (splitmix64(40 + m, n * m) & np.uint64(0xFFFFFFFF)).astype(np.uint32).reshape(n, m)
+        v = (splitmix64(41 + m, n * m) & np.uint64(0xFFFFFFFF)).astype(np.uint32).reshape(n, m)
+        for i in range(n):
+            v[i, 1 + i % m:] = 0
+            v[i, 0] |= 1
+        q1, r1, _ = oracle.div_ref(u, v)
+        q2, r2 = oracle.ref_div_u32(u, v)
+        assert (q1 == q2).all() and (r1 == r2).all()
+
+
+def test_reference_division_defect_and_exact_oracle(oracle):
+    U, V, m = REF_DIV_DEFECT
+    u = np.array([_digits(U, m)], np.uint32)
+    v = np.array([_digits(V, m)], np.uint32)
+    qf, rf, _ = oracle.div_ref(u, v)
+    assert _int(qf[0]) == U // V - 1 and _int(rf[0]) == U % V + V     # r >= v: not reduced
+    if oracle.ref_div_lib() is not None:
+        qr, rr = oracle.ref_div_u32(u, v)
+        assert _int(qr[0]) == U // V - 1
+    q, r, _ = oracle.div(u, v)
+    assert _int(q[0]) == U // V and _int(r[0]) == U % V
+
+
+def test_exact_oracle_division_random(oracle):
+    for m in (4, 5, 6, 8):
+        n = 1500
+        u = (splitmix64(70 + m, n * m) & np.uint64(0xFFFFFFFF)).astype(np.uint32).reshape(n, m)
+        v = (splitmix64(71 + m, n * m) & np.uint64(0xFFFFFFFF)).astype(np.uint32).reshape(n, m)
+        nz = 1 + np.arange(n) % m
+        for i in range(n):
+            v[i, nz[i]:] = 0
+            v[i, nz[i] - 1] |= 1
+        q, r, _ = oracle.div(u, v)
+        for i in range(n):
+            U, V = _int(u[i]), _int(v[i])
+            assert _int(q[i]) == U // V and _int(r[i]) == U % V
