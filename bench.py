@@ -5,29 +5,36 @@ Headline workload (one "step"): the batched add + signed-sub sweep over u64
 limbs at 2^10 .. 2^18 bits, each size filling 2^27 limbs per operand (1 GiB),
 80 % uniform and 20 % carry-chain instances -- 9 sizes x {add, sub} = 18
 kernel launches per step.  The metric is the reference's add bandwidth,
-GB/s = 3 * n * m * 8 / t (thesis/sections/performance.tex:75-78), summed over
-the step.  Operands are 1 GiB each, far larger than the 129 MB L2, so no L2
-flush is needed between launches.
+GB/s = 3 * n * m * 8 / t (thesis/sections/performance.tex:75-78), over the
+whole step (plus one sign byte per subtraction).  Operands are 1 GiB each,
+far larger than the 129 MB L2, so no L2 flush is needed between launches.
 
-  * value      -- device-resident inputs, whole-job GB/s over all ranks;
-  * e2e        -- the same sweep through the host C-ABI entry points
-                  (bi_host_add_u64 / bi_host_sub_u64) from pinned host memory,
-                  copies in and out inside the timed region;
-  * roofline   -- the add/sub kernel's algorithmic bytes per launch over its
-                  CUDA-event launch time, against the measured HBM copy peak;
-  * cpu_baseline -- the CPU oracle port on the host cores, on a 1/8 sample.
+  * value        -- device-resident inputs, whole-job GB/s over all ranks;
+  * e2e          -- the same sweep through the host C-ABI entry points
+                    (bi_host_add_u64 / bi_host_sub_u64) from pinned host
+                    memory, copies in and out inside the timed region;
+  * roofline     -- the add/sub kernel's algorithmic bytes per launch over
+                    its CUDA-event launch time, against the measured HBM copy
+                    peak (MEASURED_PEAKS.json), with the ncu DRAM traffic;
+  * cpu_baseline -- the CPU oracle port on all host cores, full-size inputs;
+  * extra        -- the multiply and division workloads (instances/s, word
+                    products/s against the measured integer-pipe peak).
 
 `--impl reference` times the reference's CPU implementation of the path on
-the host cores -- here the oracle port of it, all threads -- on the same
-metric and workload, and prints the same JSON line with "impl": "reference".
+the host cores -- the oracle port of it, all threads -- on the same metric
+and workload, and prints the same JSON line with "impl": "reference".
 
 Multi-GPU: instances are independent, so N ranks run N replicas of the step
-(weak scaling, no collective on the data path; NCCL is used only for the
-barrier and the max over ranks of the elapsed time).
+(weak scaling, no collective on the data path; NCCL only carries the barrier
+and the max over ranks of the elapsed time).
+
+`--workload add|sub|mul|mul2048|div` with `--bits`, `--total-limbs-log2`,
+`--mul-m`, `--div-m` runs one operation on one size (used for profiling).
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import subprocess
@@ -40,153 +47,294 @@ import numpy as np
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, "big-int_gb300"))
 
-TOTAL_LIMBS = 1 << 27
-SEED = 1001                       # workload index 1 -> seed 1000 + 1
+SEED_ADDSUB = 1001
 BITS = [1 << k for k in range(10, 19)]
-PUBLISHED_ADD_U64_GBS = 165.0     # mean of C-V3 u64 add over 2^10..2^18 bits, GTX 1650 SUPER
+PUBLISHED_ADD_U64_GBS = 165.0     # mean C-V3 u64 add over 2^10..2^18 bits, GTX 1650 SUPER
 FALLBACK_HBM_GBS = 6800.0
 
 
-def step_bytes(total_limbs: int = TOTAL_LIMBS) -> tuple[int, int]:
-    """Algorithmic bytes of one step: (add+sub limb traffic, sign bytes)."""
-    per_op = 3 * total_limbs * 8
-    signs = sum(total_limbs // (b // 64) for b in BITS)
-    return 2 * len(BITS) * per_op + signs, signs
+# ---------------------------------------------------------------------------
+# clocks during the timed region (read-only NVML queries, nvidia-smi fallback)
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, period_s: float = 0.01):
+        self.period = period_s
+        self.samples = []
+        self.stop_evt = threading.Event()
+        self.nvml = None
+        self.handle = None
+        try:
+            import torch
+
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                raise RuntimeError("nvmlInit")
+            h = ctypes.c_void_p()
+            props = torch.cuda.get_device_properties(torch.cuda.current_device())
+            bus = getattr(props, "pci_bus_id", None)
+            ok = False
+            if bus is not None:
+                busid = f"{getattr(props, 'pci_domain_id', 0):08X}:{bus:02X}:{getattr(props, 'pci_device_id', 0):02X}.0"
+                ok = nv.nvmlDeviceGetHandleByPciBusId_v2(busid.encode(), ctypes.byref(h)) == 0
+            if not ok:
+                ok = nv.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(h)) == 0
+            if ok:
+                self.nvml, self.handle = nv, h
+        except Exception:
+            self.nvml = None
+
+    def _sample_nvml(self):
+        nv, h = self.nvml, self.handle
+        sm, mx = ctypes.c_uint(), ctypes.c_uint()
+        reasons = ctypes.c_ulonglong()
+        nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(sm))
+        nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx))
+        f = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        f(h, ctypes.byref(reasons))
+        return sm.value, mx.value, reasons.value
+
+    def _loop(self):
+        while not self.stop_evt.is_set():
+            try:
+                self.samples.append(self._sample_nvml())
+            except Exception:
+                break
+            time.sleep(self.period)
+
+    def __enter__(self):
+        if self.nvml is not None:
+            self.thread = threading.Thread(target=self._loop, daemon=True)
+            self.thread.start()
+        else:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=clocks.sm,clocks.max.sm,clocks_event_reasons.active",
+                 "--format=csv,noheader,nounits", "-lms", "50"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        return self
+
+    def __exit__(self, *exc):
+        if self.nvml is not None:
+            self.stop_evt.set()
+            self.thread.join(timeout=2)
+        else:
+            self.proc.terminate()
+            out, _ = self.proc.communicate(timeout=5)
+            for line in out.splitlines():
+                f = [x.strip() for x in line.split(",")]
+                try:
+                    self.samples.append((float(f[0]), float(f[1]), int(f[2], 16)))
+                except Exception:
+                    pass
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [s[0] for s in self.samples]
+        reasons = set()
+        for _, _, r in self.samples:
+            for bit, name in self.REASONS.items():
+                if r & bit:
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(s[1] for s in self.samples)),
+                "reasons": sorted(reasons), "samples": len(self.samples),
+                "source": "nvml" if self.nvml is not None else "nvidia-smi"}
 
 
-def measured_peak():
-    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+def measured_peaks():
     try:
-        with open(path) as f:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
             d = json.load(f)
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def ncu_traffic():
-    """Per-launch DRAM bytes of the add/sub kernel from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "addsub_traffic.json")
+def ncu_traffic(name: str):
     try:
-        with open(path) as f:
-            return json.load(f)
+        with open(os.path.join(REPO, "profiles", "traffic.json")) as f:
+            return json.load(f).get(name)
     except Exception:
         return None
 
 
-class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+# ---------------------------------------------------------------------------
+# helpers
+# ---------------------------------------------------------------------------
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+def event_time(stream, fn, reps: int, warmup: int = 2):
+    import torch
 
-    def __init__(self, gpu_index: int):
-        self.gpu = gpu_index
-        self.proc = None
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
 
-    def __enter__(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
-                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-        except Exception:
-            self.proc = None
-        return self
 
-    def __exit__(self, *exc):
-        self.lines = []
-        if self.proc is not None:
-            self.proc.terminate()
-            try:
-                out, _ = self.proc.communicate(timeout=5)
-            except Exception:
-                self.proc.kill()
-                out, _ = self.proc.communicate()
-            self.lines = [l for l in out.splitlines() if l.strip()]
+def check(L, st):
+    if st != 0:
+        raise RuntimeError(f"library call failed: {L.bi_last_error().decode()}")
 
-    def summary(self):
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for l in getattr(self, "lines", []):
-            f = [x.strip() for x in l.split(",")]
-            if len(f) < 9:
-                continue
-            try:
-                sm.append(float(f[1]))
-                mx.append(float(f[2]))
-            except ValueError:
-                continue
-            for nm, v in zip(names, f[5:9]):
-                if v.lower() in ("active", "1", "yes"):
-                    reasons.add(nm)
-        if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+
+def cpu_addsub(op: str, a: np.ndarray, b: np.ndarray, nthreads: int) -> float:
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle as O
+
+    t0 = time.perf_counter()
+    if op == "add":
+        O.add(a, b, nthreads=nthreads)
+    else:
+        O.sub(a, b, nthreads=nthreads)
+    return time.perf_counter() - t0
 
 
 # ---------------------------------------------------------------------------
-# CPU legs (oracle port; the library never touches these)
+# reference arm: the reference's CPU implementation (oracle port), host cores
 # ---------------------------------------------------------------------------
 
-def cpu_sweep(nthreads: int, total_limbs: int) -> dict:
+def run_reference(args) -> None:
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle as O
     from bigint_gb300.workloads import addsub_u64
 
     O.build()
-    elapsed = 0.0
-    nbytes = 0
-    for bits in BITS:
-        for op in ("add", "sub"):
-            a, b = addsub_u64(bits, seed=SEED, total_limbs=total_limbs, op=op)
-            t0 = time.perf_counter()
-            if op == "add":
-                O.add(a, b, nthreads=nthreads)
-            else:
-                O.sub(a, b, nthreads=nthreads)
-            elapsed += time.perf_counter() - t0
-            nbytes += 3 * a.size * 8 + (a.shape[0] if op == "sub" else 0)
-    return {"gbs": nbytes / elapsed / 1e9, "seconds": elapsed, "bytes": nbytes}
-
-
-def run_reference(args) -> None:
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
     cores = os.cpu_count() or 1
-    sample = TOTAL_LIMBS // 8
+    sample_limbs = 1 << (args.total_limbs_log2 - 3)
+    data = {(bits, op): addsub_u64(bits, seed=SEED_ADDSUB, total_limbs=sample_limbs, op=op)
+            for bits in BITS for op in ("add", "sub")}
+    per_step = sum(3 * a.size * 8 + (a.shape[0] if op == "sub" else 0) for (bits, op), (a, b) in data.items())
     for _ in range(args.warmup):
-        pass  # the CPU port has no warm-up state; the first timed sweep includes page faults
-    vals = []
+        for (bits, op), (a, b) in data.items():
+            cpu_addsub(op, a, b, cores)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_sweep(cores, sample)["gbs"])
+        for (bits, op), (a, b) in data.items():
+            cpu_addsub(op, a, b, cores)
     wall = time.perf_counter() - t0
-    v = float(np.median(vals))
+    v = per_step * args.steps / wall / 1e9
     line = {
         "impl": "reference",
         "metric": "add/sub sweep GB/s (u64, 2^10..2^18 bits, 2^27 limbs per operand)",
         "value": round(v, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(1000 * wall / max(1, args.steps), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-        "data": "synthetic (splitmix64 seed 1001)",
-        "config": {"workload": "addsub_u64 sweep 2^10..2^18 bits", "sample": "1/8 of the 2^27 limbs per size",
-                   "l2": "inputs larger than L2"},
+        "data": "synthetic (splitmix64 seed 1001; 20% carry-chain instances)",
+        "config": {"workload": "addsub_u64 sweep: 9 sizes 2^10..2^18 bits x {add, sub}",
+                   "sample": f"2^{args.total_limbs_log2 - 3} limbs per operand per size (1/8 of the GPU workload)"},
         "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-                         "sample": "each step: the full 9-size add+sub sweep at 2^24 limbs per operand "
-                                   "(1/8 of the GPU workload); oracle port of ker-add.cu.h / sub.fut, "
-                                   "one pthread per core"},
+                         "sample": "each step: the 9-size add+sub sweep at 1/8 of the GPU workload's limbs; "
+                                   "the oracle port of ker-add.cu.h / sub.fut, one pthread per core"},
         "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
 # ---------------------------------------------------------------------------
-# GPU leg
+# GPU measurements
 # ---------------------------------------------------------------------------
+
+def measure_extra(B, L, stream, args):
+    """Multiply and division workloads: instances/s and word-product rates."""
+    import torch
+
+    from bigint_gb300.workloads import MUL_U64, device_uniform_u64, mul2048_u32, mul_u64_device
+
+    sp = int(stream.cuda_stream)
+    rates = B.probe_intpipe()
+    peak_wps = max(rates.values())
+    out = {"intpipe_peak_word_products_per_s": peak_wps,
+           "intpipe_peak_form": max(rates, key=rates.get)}
+    mul = {}
+    for m, n in MUL_U64:
+        a, b = mul_u64_device(m, n)
+        r = torch.empty((n, 2 * m), dtype=torch.int64, device="cuda")
+        ms = event_time(stream, lambda: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, sp)), 5)
+        rt = torch.empty((n, m), dtype=torch.int64, device="cuda")
+        ms_t = event_time(stream, lambda: check(L, L.bi_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, sp)), 5)
+        wp = n * (2 * m) ** 2
+        mul[f"m{m}_n{n}"] = {"full_instances_per_s": round(n / ms * 1e3), "full_ms": round(ms, 4),
+                             "word_products_per_s": wp / ms * 1e3, "frac_of_intpipe_peak": round(wp / ms * 1e3 / peak_wps, 4),
+                             "truncated_instances_per_s": round(n / ms_t * 1e3), "truncated_ms": round(ms_t, 4)}
+        del a, b, r, rt
+    out["mul_u64_full"] = mul
+    a, b = mul2048_u32()
+    da, db = B.to_device(a), B.to_device(b)
+    r = torch.empty((a.shape[0], 128), dtype=torch.int32, device="cuda")
+    ms = event_time(stream, lambda: check(L, L.bi_mulfull_u32(da.data_ptr(), db.data_ptr(), r.data_ptr(), 64, 4096, sp)), 20)
+    out["mul2048_u32"] = {"instances_per_s": round(4096 / ms * 1e3), "ms": round(ms, 5),
+                          "note": "4096 pairs of 64 u32 limbs, 10% all-ones, full 128-limb product"}
+    div = {}
+    for mv, n in [(4, 1 << 16), (16, 1 << 14), (64, 1 << 13), (256, 1 << 12), (1024, 1 << 10)]:
+        u = device_uniform_u64(11, n, 2 * mv)
+        v = device_uniform_u64(12, n, mv)
+        v[:, -1] |= 1
+        q = torch.empty_like(u)
+        rr = torch.empty_like(v)
+        st = torch.empty(n, dtype=torch.uint8, device="cuda")
+        ms = event_time(stream, lambda: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
+                                                               st.data_ptr(), 2 * mv, mv, n, sp)), 3, 1)
+        div[f"m{mv}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4)}
+        del u, v, q, rr, st
+    out["div_u64_2m_by_m"] = div
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_single(args) -> None:
+    """One operation on one size (for profiling); prints a small JSON line."""
+    import torch
+
+    import bigint_gb300 as B
+    from bigint_gb300.workloads import addsub_u64_device, device_uniform_u64, mul_u64_device
+
+    B.build()
+    L = B.lib()
+    stream = torch.cuda.current_stream()
+    sp = int(stream.cuda_stream)
+    w = args.workload
+    if w in ("add", "sub"):
+        bits = args.bits or 65536
+        a, b = addsub_u64_device(bits, seed=SEED_ADDSUB, total_limbs=1 << args.total_limbs_log2, op=w)
+        n, m = a.shape
+        r = torch.empty_like(a)
+        s = torch.empty(n, dtype=torch.uint8, device="cuda")
+        fn = (lambda: check(L, L.bi_add_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, sp))) if w == "add" else \
+             (lambda: check(L, L.bi_sub_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), s.data_ptr(), m, n, sp)))
+        ms = event_time(stream, fn, args.steps, args.warmup)
+        print(json.dumps({"workload": w, "bits": bits, "n": n, "ms": ms, "GBps": 3 * n * m * 8 / ms / 1e6}))
+    elif w == "mul":
+        m = args.mul_m
+        n = max(1, (1 << args.total_limbs_log2) // m)
+        a, b = mul_u64_device(m, n)
+        r = torch.empty((n, 2 * m), dtype=torch.int64, device="cuda")
+        ms = event_time(stream, lambda: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, sp)),
+                        args.steps, args.warmup)
+        print(json.dumps({"workload": w, "m": m, "n": n, "ms": ms, "word_products_per_s": n * 4 * m * m / ms * 1e3}))
+    elif w == "div":
+        mv = args.div_m
+        n = max(1, (1 << args.total_limbs_log2) // (2 * mv))
+        u = device_uniform_u64(11, n, 2 * mv)
+        v = device_uniform_u64(12, n, mv)
+        v[:, -1] |= 1
+        q, rr = torch.empty_like(u), torch.empty_like(v)
+        st = torch.empty(n, dtype=torch.uint8, device="cuda")
+        ms = event_time(stream, lambda: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
+                                                               st.data_ptr(), 2 * mv, mv, n, sp)), args.steps, args.warmup)
+        print(json.dumps({"workload": w, "m": mv, "n": n, "ms": ms, "instances_per_s": n / ms * 1e3}))
+    else:
+        raise SystemExit(f"unknown workload {w}")
+
 
 def run_ours(args) -> None:
     import torch
@@ -206,116 +354,111 @@ def run_ours(args) -> None:
     L = B.lib()
     stream = torch.cuda.current_stream()
     sp = int(stream.cuda_stream)
+    total = 1 << args.total_limbs_log2
+    bits_list = [args.bits] if args.bits else BITS
 
-    # ---- device-resident inputs for every size and op
-    inputs = {}
-    for bits in BITS:
-        for op in ("add", "sub"):
-            inputs[(bits, op)] = addsub_u64_device(bits, seed=SEED, total_limbs=TOTAL_LIMBS, op=op)
-    out = torch.empty(TOTAL_LIMBS, dtype=torch.int64, device="cuda")
-    sign = torch.empty(TOTAL_LIMBS // 16, dtype=torch.uint8, device="cuda")
+    inputs = {(bits, op): addsub_u64_device(bits, seed=SEED_ADDSUB, total_limbs=total, op=op)
+              for bits in bits_list for op in ("add", "sub")}
+    out = torch.empty(total, dtype=torch.int64, device="cuda")
+    sign = torch.empty(total // 16, dtype=torch.uint8, device="cuda")
     torch.cuda.synchronize()
 
     def launch(bits, op):
         a, b = inputs[(bits, op)]
         n, m = a.shape
         if op == "add":
-            st = L.bi_add_u64(a.data_ptr(), b.data_ptr(), out.data_ptr(), m, n, sp)
+            check(L, L.bi_add_u64(a.data_ptr(), b.data_ptr(), out.data_ptr(), m, n, sp))
         else:
-            st = L.bi_sub_u64(a.data_ptr(), b.data_ptr(), out.data_ptr(), sign.data_ptr(), m, n, sp)
-        if st != 0:
-            raise RuntimeError(f"launch failed: {L.bi_last_error().decode()}")
+            check(L, L.bi_sub_u64(a.data_ptr(), b.data_ptr(), out.data_ptr(), sign.data_ptr(), m, n, sp))
 
-    def one_step(events=None):
-        for bits in BITS:
-            for op in ("add", "sub"):
-                if events is not None:
-                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    e0.record(stream)
-                    launch(bits, op)
-                    e1.record(stream)
-                    events.append((bits, op, e0, e1))
-                else:
-                    launch(bits, op)
+    per_step = 0
+    for (bits, op), (a, b) in inputs.items():
+        per_step += 3 * a.numel() * 8 + (a.shape[0] if op == "sub" else 0)
 
-    for _ in range(max(3, args.warmup)):
-        one_step()
+    warm = max(3, args.warmup)
+    for _ in range(warm):
+        for key in inputs:
+            launch(*key)
     torch.cuda.synchronize()
 
-    # ---- timed region (device-resident)
     events = []
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    with ClockSampler() as clk:
         start.record(stream)
         for _ in range(args.steps):
-            one_step(events)
+            for key in inputs:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                launch(*key)
+                e1.record(stream)
+                events.append((key, e0, e1))
         stop.record(stream)
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    elapsed_ms = start.elapsed_time(stop)
-    t = torch.tensor([elapsed_ms], device="cuda")
+    t = torch.tensor([start.elapsed_time(stop)], device="cuda")
     if world > 1:
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
     elapsed_ms = float(t.item())
-    launches = len(events)
+    value = per_step * args.steps * world / (elapsed_ms / 1e3) / 1e9
 
-    per_step, signs = step_bytes()
-    total_bytes = per_step * args.steps * world
-    value = total_bytes / (elapsed_ms / 1e3) / 1e9
-
-    kern_ms = [e0.elapsed_time(e1) for (_, _, e0, e1) in events]
     per_launch = {}
-    for (bits, op, e0, e1), ms in zip(events, kern_ms):
-        per_launch.setdefault(f"{op}_{bits}", []).append(ms)
-    avg_launch_ms = float(np.mean(kern_ms))
-    bytes_per_launch = per_step / (2 * len(BITS))
+    for (bits, op), e0, e1 in events:
+        per_launch.setdefault(f"{op}_{bits}", []).append(e0.elapsed_time(e1))
+    launch_ms = [x for v in per_launch.values() for x in v]
+    avg_launch_ms = float(np.mean(launch_ms))
+    bytes_per_launch = per_step / len(inputs)
     achieved = bytes_per_launch / (avg_launch_ms / 1e3) / 1e9
-    peak, peak_kind = measured_peak()
-    traffic = ncu_traffic()
+    peak, peak_kind = measured_peaks()
 
-    # ---- e2e through the host C-ABI entry points (pinned host memory)
+    # ---- e2e through the host C-ABI entry points, and the CPU baseline on the same host buffers
     e2e_ms = 0.0
     h2d = d2h = 0
-    hr =torch.empty(TOTAL_LIMBS, dtype=torch.int64, pin_memory=True)
-    hs = torch.empty(TOTAL_LIMBS // 16, dtype=torch.uint8, pin_memory=True)
-    ha = torch.empty(TOTAL_LIMBS, dtype=torch.int64, pin_memory=True)
-    hb = torch.empty(TOTAL_LIMBS, dtype=torch.int64, pin_memory=True)
-    e2e_steps = max(1, min(args.steps, 2))
-    for _ in range(e2e_steps):
-        for bits in BITS:
-            for op in ("add", "sub"):
-                a, b = inputs[(bits, op)]
-                n, m = a.shape
-                ha.copy_(a.view(-1))
-                hb.copy_(b.view(-1))
-                torch.cuda.synchronize()
+    cpu_s = 0.0
+    cpu_bytes = 0
+    nthreads = os.cpu_count() or 1
+    ha = torch.empty(total, dtype=torch.int64, pin_memory=True)
+    hb = torch.empty(total, dtype=torch.int64, pin_memory=True)
+    hr = torch.empty(total, dtype=torch.int64, pin_memory=True)
+    hs = torch.empty(total // 16, dtype=torch.uint8, pin_memory=True)
+    e2e_steps = 0 if args.no_e2e else 1
+    cpu_reps = 0 if (args.no_cpu or rank != 0) else 2
+    for rep in range(max(e2e_steps, cpu_reps)):
+        for (bits, op), (a, b) in inputs.items():
+            n, m = a.shape
+            ha[: n * m].copy_(a.view(-1))
+            hb[: n * m].copy_(b.view(-1))
+            torch.cuda.synchronize()
+            if rep < e2e_steps:
                 t0 = time.perf_counter()
                 if op == "add":
-                    st = L.bi_host_add_u64(ha.data_ptr(), hb.data_ptr(), hr.data_ptr(), m, n)
+                    check(L, L.bi_host_add_u64(ha.data_ptr(), hb.data_ptr(), hr.data_ptr(), m, n))
                     d2h += n * m * 8
                 else:
-                    st = L.bi_host_sub_u64(ha.data_ptr(), hb.data_ptr(), hr.data_ptr(), hs.data_ptr(), m, n)
+                    check(L, L.bi_host_sub_u64(ha.data_ptr(), hb.data_ptr(), hr.data_ptr(), hs.data_ptr(), m, n))
                     d2h += n * m * 8 + n
                 e2e_ms += (time.perf_counter() - t0) * 1e3
                 h2d += 2 * n * m * 8
-                if st != 0:
-                    raise RuntimeError(L.bi_last_error().decode())
-    e2e_t = torch.tensor([e2e_ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = per_step * e2e_steps * world / (float(e2e_t.item()) / 1e3) / 1e9
+            if rep < cpu_reps:
+                an = ha[: n * m].numpy().view(np.uint64).reshape(n, m)
+                bn = hb[: n * m].numpy().view(np.uint64).reshape(n, m)
+                cpu_s += cpu_addsub(op, an, bn, nthreads)
+                cpu_bytes += 3 * n * m * 8 + (n if op == "sub" else 0)
+    e2e = None
+    if e2e_steps:
+        e2e_t = torch.tensor([e2e_ms], device="cuda")
+        if world > 1:
+            dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+        e2e = {"value": round(per_step * e2e_steps * world / (float(e2e_t.item()) / 1e3) / 1e9, 2), "unit": "GB/s",
+               "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
+               "path": "bi_host_add_u64 / bi_host_sub_u64 (chunked, 3-stream pipeline) from pinned host buffers"}
 
-    cpu = None
-    if rank == 0:
-        nthreads = os.cpu_count() or 1
-        r = cpu_sweep(nthreads, TOTAL_LIMBS // 8)
-        cpu = {"value": round(r["gbs"], 3), "unit": "GB/s", "cores": nthreads, "kind": "port",
-               "sample": "the 9-size add+sub sweep at 2^24 limbs per operand (1/8 of the workload), "
-                         f"{r['seconds']:.2f} s of CPU time; oracle port, one pthread per core"}
+    extra = None
+    if not args.no_extras:
+        extra = measure_extra(B, L, stream, args)
 
     if rank == 0:
         line = {
@@ -324,31 +467,33 @@ def run_ours(args) -> None:
             "unit": "GB/s",
             "n_gpus": world,
             "steps": args.steps,
-            "warmup": max(3, args.warmup),
+            "warmup": warm,
             "ms_per_step": round(elapsed_ms / args.steps, 4),
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": round(value / PUBLISHED_ADD_U64_GBS, 2),
+            "vs_baseline_ref": "u64 add C-V3 mean 165 GB/s, GTX 1650 SUPER (thesis performance.tex:181-198)",
             "dtype": "u64",
             "data": "synthetic (splitmix64 seed 1001; 20% carry-chain instances)",
-            "config": {"workload": "addsub_u64 sweep: 9 sizes 2^10..2^18 bits x {add, sub}, "
-                                   "n = 2^27/m instances per size",
+            "config": {"workload": "addsub_u64 sweep: 9 sizes 2^10..2^18 bits x {add, sub}, n = 2^27/m instances per size",
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (1 GiB per operand), no flush"},
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)"
-                         if peak_kind == "measured" else "fallback 6.8 TB/s",
-                         "kernel": "addsub_kernel", "bytes_per_launch": int(bytes_per_launch),
+                         "frac": round(achieved / peak, 4),
+                         "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+                         else "of fallback 6.8 TB/s",
+                         "kernel": "addsub_kernel (add and sub launches)", "bytes_per_launch": int(bytes_per_launch),
                          "avg_launch_ms": round(avg_launch_ms, 5),
-                         "traffic": (traffic or {}).get("bytes_per_launch")},
-            "per_size_gbs": {k: round(3 * TOTAL_LIMBS * 8 / (np.mean(v) / 1e3) / 1e9, 1)
-                             for k, v in per_launch.items()},
-            "e2e": {"value": round(e2e_value, 2), "unit": "GB/s",
-                    "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
-                    "path": "bi_host_add_u64 / bi_host_sub_u64 from pinned host buffers"},
-            "gpu_launches": launches,
+                         "traffic": ncu_traffic("addsub_kernel")},
+            "per_size_gbs": {k: round(3 * total * 8 / (float(np.mean(v)) / 1e3) / 1e9, 1) for k, v in per_launch.items()},
+            "e2e": e2e,
+            "gpu_launches": len(events),
             "clocks": clk.summary(),
-            "cpu_baseline": cpu,
+            "cpu_baseline": None if not cpu_reps else {
+                "value": round(cpu_bytes / cpu_s / 1e9, 3), "unit": "GB/s", "cores": nthreads, "kind": "port",
+                "sample": f"the full sweep (same inputs, 2^27 limbs per size) run {cpu_reps}x: {cpu_s:.2f} s wall "
+                          f"on {nthreads} threads; oracle port of ker-add.cu.h / sub.fut"},
+            "extra": extra,
         }
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -358,12 +503,22 @@ def run_ours(args) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="addsub", choices=["addsub", "add", "sub", "mul", "div"])
+    ap.add_argument("--bits", type=int, default=0, help="restrict the add/sub sweep to one size")
+    ap.add_argument("--total-limbs-log2", type=int, default=27)
+    ap.add_argument("--mul-m", type=int, default=1024)
+    ap.add_argument("--div-m", type=int, default=256)
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "addsub":
+        run_single(args)
     else:
         run_ours(args)
 

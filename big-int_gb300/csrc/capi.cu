@@ -36,27 +36,6 @@ int num_sms() {
     return sms;
 }
 
-// RAII device buffer used only by the host-pointer entry points.
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-    ~DevBuf() {
-        if (p) cudaFree(p);
-    }
-    bi_status alloc(size_t nbytes) {
-        bytes = nbytes;
-        if (nbytes == 0) return BI_OK;
-        cudaError_t e = cudaMalloc(&p, nbytes);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            cudaGetLastError();
-            return set_error(e == cudaErrorMemoryAllocation ? BI_ENOMEM : BI_ECUDA,
-                             "cudaMalloc(%zu): %s", nbytes, cudaGetErrorString(e));
-        }
-        return BI_OK;
-    }
-};
-
 static bi_status cuda_ok(cudaError_t e, const char* what) {
     if (e == cudaSuccess) return BI_OK;
     cudaGetLastError();
@@ -69,25 +48,89 @@ static bi_status cuda_ok(cudaError_t e, const char* what) {
         if (_s != BI_OK) return _s;    \
     } while (0)
 
+// Host-pointer entry points run the batch as a pipeline: the instances are
+// cut into chunks of about PIPE_CHUNK_BYTES of the first operand; chunk c
+// goes to stream c % PIPE_STREAMS, which copies its inputs in, runs the
+// kernel and copies its outputs out, so the copies of one chunk overlap the
+// kernels and copies of the others.  Device chunk buffers come from the
+// stream-ordered allocator and are returned when the call ends.
+constexpr size_t PIPE_CHUNK_BYTES = 32ull << 20;
+constexpr int PIPE_STREAMS = 3;
+
+struct HostIO {
+    const void* in[2];        // host inputs (per-instance sizes in bytes below)
+    size_t in_bytes[2];
+    void* out[3];             // host outputs (two limb arrays and one byte array)
+    size_t out_bytes[3];
+};
+
+template <typename Launch>
+static bi_status host_pipelined(const HostIO& io, uint64_t n, Launch launch) {
+    if (n == 0) return BI_OK;
+    const size_t per = io.in_bytes[0] ? io.in_bytes[0] : 1;
+    uint64_t chunk = PIPE_CHUNK_BYTES / per;
+    if (chunk < 1) chunk = 1;
+    if (chunk > n) chunk = n;
+    const uint64_t nchunks = (n + chunk - 1) / chunk;
+    const int ns = nchunks < (uint64_t)PIPE_STREAMS ? (int)nchunks : PIPE_STREAMS;
+
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t keep = 4ull << 30;   // keep chunk buffers cached between calls of this process
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaStream_t st[PIPE_STREAMS] = {};
+    void* dbuf[PIPE_STREAMS][5] = {};
+    bi_status rs = BI_OK;
+    for (int k = 0; k < ns && rs == BI_OK; k++) {
+        cudaError_t e = cudaStreamCreateWithFlags(&st[k], cudaStreamNonBlocking);
+        if (e != cudaSuccess) { st[k] = nullptr; rs = cuda_ok(e, "stream create"); break; }
+        for (int j = 0; j < 2 && rs == BI_OK; j++)
+            if (io.in_bytes[j]) rs = cuda_ok(cudaMallocAsync(&dbuf[k][j], io.in_bytes[j] * chunk, st[k]), "chunk alloc");
+        for (int j = 0; j < 3 && rs == BI_OK; j++)
+            if (io.out_bytes[j]) rs = cuda_ok(cudaMallocAsync(&dbuf[k][2 + j], io.out_bytes[j] * chunk, st[k]), "chunk alloc");
+    }
+    for (uint64_t c = 0; c < nchunks && rs == BI_OK; c++) {
+        const int k = (int)(c % ns);
+        const uint64_t i0 = c * chunk;
+        const uint64_t cnt = n - i0 < chunk ? n - i0 : chunk;
+        for (int j = 0; j < 2 && rs == BI_OK; j++)
+            if (io.in_bytes[j])
+                rs = cuda_ok(cudaMemcpyAsync(dbuf[k][j], (const char*)io.in[j] + i0 * io.in_bytes[j],
+                                             cnt * io.in_bytes[j], cudaMemcpyHostToDevice, st[k]), "copy in");
+        if (rs == BI_OK) rs = launch(dbuf[k][0], dbuf[k][1], dbuf[k][2], dbuf[k][3], (uint8_t*)dbuf[k][4], cnt, st[k]);
+        for (int j = 0; j < 3 && rs == BI_OK; j++)
+            if (io.out_bytes[j] && io.out[j])
+                rs = cuda_ok(cudaMemcpyAsync((char*)io.out[j] + i0 * io.out_bytes[j], dbuf[k][2 + j],
+                                             cnt * io.out_bytes[j], cudaMemcpyDeviceToHost, st[k]), "copy out");
+    }
+    for (int k = 0; k < ns; k++) {
+        if (!st[k]) continue;
+        for (int j = 0; j < 5; j++)
+            if (dbuf[k][j]) cudaFreeAsync(dbuf[k][j], st[k]);
+        cudaError_t e = cudaStreamSynchronize(st[k]);
+        if (rs == BI_OK && e != cudaSuccess) rs = cuda_ok(e, "pipeline");
+        cudaStreamDestroy(st[k]);
+    }
+    return rs;
+}
+
 template <typename T, typename Launch>
 static bi_status host_binary(const T* ha, const T* hb, T* hr, uint8_t* hsign, uint32_t m, uint64_t n,
                              size_t out_limbs_per_inst, Launch launch) {
     if (n == 0) return BI_OK;
     if (m == 0) return set_error(BI_EINVAL, "m must be >= 1");
     if (!ha || !hb || !hr) return set_error(BI_EINVAL, "NULL host buffer");
-    const size_t in_bytes = (size_t)n * m * sizeof(T);
-    const size_t out_bytes = (size_t)n * out_limbs_per_inst * sizeof(T);
-    DevBuf da, db, dr, ds;
-    BI_TRY(da.alloc(in_bytes));
-    BI_TRY(db.alloc(in_bytes));
-    BI_TRY(dr.alloc(out_bytes));
-    if (hsign) BI_TRY(ds.alloc(n));
-    BI_TRY(cuda_ok(cudaMemcpy(da.p, ha, in_bytes, cudaMemcpyHostToDevice), "copy a"));
-    BI_TRY(cuda_ok(cudaMemcpy(db.p, hb, in_bytes, cudaMemcpyHostToDevice), "copy b"));
-    BI_TRY(launch((const T*)da.p, (const T*)db.p, (T*)dr.p, (uint8_t*)ds.p));
-    BI_TRY(cuda_ok(cudaMemcpy(hr, dr.p, out_bytes, cudaMemcpyDeviceToHost), "copy r"));
-    if (hsign) BI_TRY(cuda_ok(cudaMemcpy(hsign, ds.p, n, cudaMemcpyDeviceToHost), "copy sign"));
-    return BI_OK;
+    HostIO io = {};
+    io.in[0] = ha; io.in_bytes[0] = (size_t)m * sizeof(T);
+    io.in[1] = hb; io.in_bytes[1] = (size_t)m * sizeof(T);
+    io.out[0] = hr; io.out_bytes[0] = out_limbs_per_inst * sizeof(T);
+    io.out[2] = hsign; io.out_bytes[2] = hsign ? 1 : 0;
+    return host_pipelined(io, n, [&](void* da, void* db, void* dr, void*, uint8_t* ds, uint64_t cnt, cudaStream_t s) {
+        return launch((const T*)da, (const T*)db, (T*)dr, ds, cnt, s);
+    });
 }
 
 template <typename T>
@@ -96,22 +139,6 @@ static bi_status host_div(const T* hu, const T* hv, T* hq, T* hr, uint8_t* hstat
     if (n == 0) return BI_OK;
     if (mu == 0 || mv == 0 || mv > mu) return set_error(BI_EINVAL, "need 1 <= mv <= mu");
     if (!hu || !hv || !hq || !hr) return set_error(BI_EINVAL, "NULL host buffer");
-    DevBuf du, dv, dq, dr, ds;
-    BI_TRY(du.alloc((size_t)n * mu * sizeof(T)));
-    BI_TRY(dv.alloc((size_t)n * mv * sizeof(T)));
-    BI_TRY(dq.alloc((size_t)n * mu * sizeof(T)));
-    BI_TRY(dr.alloc((size_t)n * mv * sizeof(T)));
-    BI_TRY(ds.alloc(n));
-    BI_TRY(cuda_ok(cudaMemcpy(du.p, hu, du.bytes, cudaMemcpyHostToDevice), "copy u"));
-    BI_TRY(cuda_ok(cudaMemcpy(dv.p, hv, dv.bytes, cudaMemcpyHostToDevice), "copy v"));
-    bi_status st;
-    if constexpr (sizeof(T) == 8)
-        st = bi_div_u64((const T*)du.p, (const T*)dv.p, (T*)dq.p, (T*)dr.p, (uint8_t*)ds.p, mu, mv, n, nullptr);
-    else
-        st = bi_div_u32((const T*)du.p, (const T*)dv.p, (T*)dq.p, (T*)dr.p, (uint8_t*)ds.p, mu, mv, n, nullptr);
-    BI_TRY(st);
-    BI_TRY(cuda_ok(cudaMemcpy(hq, dq.p, dq.bytes, cudaMemcpyDeviceToHost), "copy q"));
-    BI_TRY(cuda_ok(cudaMemcpy(hr, dr.p, dr.bytes, cudaMemcpyDeviceToHost), "copy r"));
     uint8_t* stat = hstatus;
     uint8_t* own = nullptr;
     if (!stat) {
@@ -119,7 +146,19 @@ static bi_status host_div(const T* hu, const T* hv, T* hq, T* hr, uint8_t* hstat
         if (!own) return set_error(BI_ENOMEM, "host status buffer");
         stat = own;
     }
-    bi_status rs = cuda_ok(cudaMemcpy(stat, ds.p, n, cudaMemcpyDeviceToHost), "copy status");
+    HostIO io = {};
+    io.in[0] = hu; io.in_bytes[0] = (size_t)mu * sizeof(T);
+    io.in[1] = hv; io.in_bytes[1] = (size_t)mv * sizeof(T);
+    io.out[0] = hq; io.out_bytes[0] = (size_t)mu * sizeof(T);
+    io.out[1] = hr; io.out_bytes[1] = (size_t)mv * sizeof(T);
+    io.out[2] = stat; io.out_bytes[2] = 1;
+    bi_status rs = host_pipelined(io, n, [&](void* du, void* dv, void* dq, void* dr, uint8_t* ds, uint64_t cnt,
+                                             cudaStream_t s) {
+        if constexpr (sizeof(T) == 8)
+            return bi_div_u64((const T*)du, (const T*)dv, (T*)dq, (T*)dr, ds, mu, mv, cnt, s);
+        else
+            return bi_div_u32((const T*)du, (const T*)dv, (T*)dq, (T*)dr, ds, mu, mv, cnt, s);
+    });
     if (rs == BI_OK) {
         for (uint64_t i = 0; i < n; i++) {
             if (stat[i] == 1) { rs = set_error(BI_EDIV0, "instance %llu has a zero divisor", (unsigned long long)i); break; }
@@ -164,53 +203,53 @@ int bi_version(void) { return 100; }
 
 bi_status bi_host_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n) {
     return host_binary<uint64_t>(a, b, r, nullptr, m, n, m,
-        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*) {
-            return bi_add_u64(da, db, dr, m, n, nullptr);
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return bi_add_u64(da, db, dr, m, cnt, cs);
         });
 }
 bi_status bi_host_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n) {
     return host_binary<uint32_t>(a, b, r, nullptr, m, n, m,
-        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*) {
-            return bi_add_u32(da, db, dr, m, n, nullptr);
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return bi_add_u32(da, db, dr, m, cnt, cs);
         });
 }
 bi_status bi_host_sub_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* sign, uint32_t m,
                           uint64_t n) {
     return host_binary<uint64_t>(a, b, r, sign, m, n, m,
-        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t* ds) {
-            return bi_sub_u64(da, db, dr, ds, m, n, nullptr);
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t* ds, uint64_t cnt, cudaStream_t cs) {
+            return bi_sub_u64(da, db, dr, ds, m, cnt, cs);
         });
 }
 bi_status bi_host_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* sign, uint32_t m,
                           uint64_t n) {
     return host_binary<uint32_t>(a, b, r, sign, m, n, m,
-        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t* ds) {
-            return bi_sub_u32(da, db, dr, ds, m, n, nullptr);
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t* ds, uint64_t cnt, cudaStream_t cs) {
+            return bi_sub_u32(da, db, dr, ds, m, cnt, cs);
         });
 }
 
 bi_status bi_host_mul_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n) {
     return host_binary<uint64_t>(a, b, r, nullptr, m, n, m,
-        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*) {
-            return bi_mul_u64(da, db, dr, m, n, nullptr);
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return bi_mul_u64(da, db, dr, m, cnt, cs);
         });
 }
 bi_status bi_host_mul_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n) {
     return host_binary<uint32_t>(a, b, r, nullptr, m, n, m,
-        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*) {
-            return bi_mul_u32(da, db, dr, m, n, nullptr);
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return bi_mul_u32(da, db, dr, m, cnt, cs);
         });
 }
 bi_status bi_host_mulfull_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n) {
     return host_binary<uint64_t>(a, b, r, nullptr, m, n, 2 * (size_t)m,
-        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*) {
-            return bi_mulfull_u64(da, db, dr, m, n, nullptr);
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return bi_mulfull_u64(da, db, dr, m, cnt, cs);
         });
 }
 bi_status bi_host_mulfull_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n) {
     return host_binary<uint32_t>(a, b, r, nullptr, m, n, 2 * (size_t)m,
-        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*) {
-            return bi_mulfull_u32(da, db, dr, m, n, nullptr);
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return bi_mulfull_u32(da, db, dr, m, cnt, cs);
         });
 }
 

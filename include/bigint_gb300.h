@@ -13,9 +13,11 @@
  *     cudaStream_t passed as bi_stream; NULL means the legacy default
  *     stream); they are asynchronous with respect to the host and
  *     stream-ordered, and they allocate no memory;
- *   - host entry points (bi_host_*) take host pointers, allocate device
- *     buffers, copy, launch, copy back and free, synchronously -- the shape
- *     of the reference's gpuAdd/gpuMultiply wrappers;
+ *   - host entry points (bi_host_*) take host pointers and return when the
+ *     results are back in host memory -- the shape of the reference's
+ *     gpuAdd/gpuMultiply wrappers; internally the batch is cut into chunks
+ *     whose copies in, kernels and copies out overlap on three streams
+ *     (pinned host buffers get the full link bandwidth);
  *   - n == 0 is a no-op; m == 0 or a NULL buffer with n > 0 is BI_EINVAL;
  *   - any n is accepted: unlike the reference launch (grid = n/ipb, which
  *     drops the remainder, cuda/main.cu:135,307) every instance is computed;
@@ -123,7 +125,7 @@ bi_status bi_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t
                      bi_stream stream);
 
 /* ---------------------------------------------------------------------- */
-/* Host-pointer twins of the above (synchronous; allocate per call).       */
+/* Host-pointer twins of the above (synchronous, pipelined; see top).     */
 /* Mirror gpuAdd<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:108-110) and */
 /* gpuMultiply<Base,m,v>(n, h_as, h_bs, h_rs) (cuda/main.cu:280-282).      */
 /* ---------------------------------------------------------------------- */
