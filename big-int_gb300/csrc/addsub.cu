@@ -67,14 +67,57 @@ struct GP {
     uint32_t g, p;
 };
 
+// Per-row position bookkeeping of a lane's VEC limbs: which limbs start an
+// instance (seg), which end one (last), and the instance index (within the
+// tile) of the lane's first valid limb.  One division per row and lane.
+template <int VEC>
+__device__ __forceinline__ void row_positions(int li0, int len, uint32_t m, const FastDiv& mdiv, uint32_t& seg,
+                                              uint32_t& last, uint32_t& valid, uint32_t& q0, uint32_t& wrapbits) {
+    seg = last = valid = wrapbits = 0;
+    q0 = 0;
+    if (li0 + VEC <= 0 || li0 >= len) return;
+    if (m >= (uint32_t)VEC && li0 >= 0) {
+        q0 = mdiv.div((uint32_t)li0);
+        uint32_t pos = (uint32_t)li0 - q0 * m;
+#pragma unroll
+        for (int e = 0; e < VEC; e++) {
+            if (e > 0) {
+                pos++;
+                if (pos == m) { pos = 0; wrapbits |= 1u << e; }
+            }
+            if (li0 + e < len) {
+                valid |= 1u << e;
+                if (pos == 0) seg |= 1u << e;
+                if (pos == m - 1) last |= 1u << e;
+            }
+        }
+    } else {
+        // tiny m or a lane straddling the tile start: per-limb division
+        bool first = true;
+#pragma unroll
+        for (int e = 0; e < VEC; e++) {
+            const int li = li0 + e;
+            if (li < 0 || li >= len) continue;
+            const uint32_t q = mdiv.div((uint32_t)li);
+            const uint32_t pos = (uint32_t)li - q * m;
+            if (first) { q0 = q; first = false; }
+            else if (q != q0) wrapbits |= 1u << e;   // (only used when m >= VEC)
+            valid |= 1u << e;
+            if (pos == 0) seg |= 1u << e;
+            if (pos == m - 1) last |= 1u << e;
+        }
+    }
+}
+
 template <typename T, int WARPS, int ROWS, int VEC, int OP>
-__global__ void __launch_bounds__(WARPS * 32)
+__global__ void __launch_bounds__(WARPS * 32, 1024 / (WARPS * 32))
 addsub_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t m, uint64_t n,
               uint32_t ipt, FastDiv mdiv, uint64_t ntiles) {
     constexpr int ROWL = 32 * VEC;              // limbs per warp row
     constexpr int TILE = WARPS * ROWS * ROWL;   // limbs per CTA tile
-    constexpr int NCH = (OP == OP_SUB) ? 2 : 1; // carry chains
+    constexpr int NCH = (OP == OP_SUB) ? 2 : 1; // carry chains (sub: a-b and b-a)
     constexpr T HI = Limb<T>::HIGHEST;
+    static_assert(ROWS * VEC <= 32, "per-limb bit masks hold 32 limbs");
 
     __shared__ uint32_t s_gp[NCH][WARPS];       // per-warp composite, bit0 = g, bit1 = p
     __shared__ uint32_t s_first[WARPS];         // 1 if the warp's first limb starts an instance
@@ -92,26 +135,41 @@ addsub_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t m, uint6
         const int off = (int)(start & (VEC - 1));       // limbs before start in the first vector
         const uint64_t abase = start - off;
 
-        T av[ROWS][VEC], bv[ROWS][VEC];
+        // d = a + b (add) or a - b (sub), both without carries; gbits = carry
+        // (borrow) generated by each limb on its own
+        T d[ROWS][VEC];
+        uint32_t gbits = 0, segbits = 0, lastbits = 0, validbits = 0;
 
-        // ---- load: whole vectors where possible, single limbs at the edges
 #pragma unroll
         for (int rr = 0; rr < ROWS; rr++) {
             const int vi = (int)((warp * ROWS + rr) * 32 + lane);
             const int li0 = vi * VEC - off;
             const uint64_t gi = abase + (uint64_t)vi * VEC;
+            T x[VEC], y[VEC];
             if (li0 >= 0 && li0 + VEC <= len) {
-                load_limbs<T, VEC>(a + gi, av[rr]);
-                load_limbs<T, VEC>(b + gi, bv[rr]);
+                load_limbs<T, VEC>(a + gi, x);
+                load_limbs<T, VEC>(b + gi, y);
             } else {
 #pragma unroll
                 for (int e = 0; e < VEC; e++) {
                     const int li = li0 + e;
                     const bool ok = li >= 0 && li < len;
-                    av[rr][e] = ok ? __ldcs(a + gi + e) : (T)0;
-                    bv[rr][e] = ok ? __ldcs(b + gi + e) : (T)0;
+                    x[e] = ok ? __ldcs(a + gi + e) : (T)0;
+                    y[e] = ok ? __ldcs(b + gi + e) : (T)0;
                 }
             }
+#pragma unroll
+            for (int e = 0; e < VEC; e++) {
+                uint32_t g;
+                if (OP == OP_ADD) { d[rr][e] = x[e] + y[e]; g = d[rr][e] < x[e]; }
+                else              { d[rr][e] = x[e] - y[e]; g = x[e] < y[e]; }
+                gbits |= g << (rr * VEC + e);
+            }
+            uint32_t sg, la, va, q0, wr;
+            row_positions<VEC>(li0, len, m, mdiv, sg, la, va, q0, wr);
+            segbits |= sg << (rr * VEC);
+            lastbits |= la << (rr * VEC);
+            validbits |= va << (rr * VEC);
         }
 
         // ---- per-row lane classes and row ballots
@@ -119,38 +177,26 @@ addsub_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t m, uint6
         uint32_t rowS0 = 0;   // bit rr: lane 0 of row rr starts an instance
 #pragma unroll
         for (int rr = 0; rr < ROWS; rr++) {
-            const int vi = (int)((warp * ROWS + rr) * 32 + lane);
-            const int li0 = vi * VEC - off;
             GP lg[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++) { lg[c].g = 0; lg[c].p = 1; }
-            bool seg0 = false;
 #pragma unroll
             for (int e = 0; e < VEC; e++) {
-                const int li = li0 + e;
-                const bool ok = li >= 0 && li < len;
-                const bool seg = ok && (li - (int)(mdiv.div((uint32_t)li) * m) == 0);
-                if (e == 0) seg0 = seg;
-                const T x = av[rr][e], y = bv[rr][e];
-                uint32_t g0, g1 = 0, p;
-                if (OP == OP_ADD) {
-                    const T s = x + y;
-                    g0 = ok && (s < x);
-                    p = ok && (s == HI);
-                } else {
-                    g0 = ok && (x < y);   // borrow generated by a - b
-                    g1 = ok && (y < x);   // borrow generated by b - a
-                    p = ok && (x == y);   // borrow propagated by either
-                }
+                const int bit = rr * VEC + e;
+                const uint32_t ok = (validbits >> bit) & 1u;
+                const uint32_t seg = (segbits >> bit) & 1u;
+                const uint32_t g0 = ok & (gbits >> bit);
+                const uint32_t p = ok & (uint32_t)(OP == OP_ADD ? d[rr][e] == HI : d[rr][e] == 0);
 #pragma unroll
                 for (int c = 0; c < NCH; c++) {
                     if (e > 0 && seg) { lg[c].g = 0; lg[c].p = 0; }
-                    const uint32_t ge = (c == 0) ? g0 : g1;
+                    // b - a borrows where a - b neither borrows nor is zero
+                    const uint32_t ge = (c == 0) ? g0 : (ok & ~g0 & ~p & 1u);
                     lg[c].g = ge | (p & lg[c].g);
                     lg[c].p = p & lg[c].p;
                 }
             }
-            const uint32_t S = __ballot_sync(0xffffffffu, seg0);
+            const uint32_t S = __ballot_sync(0xffffffffu, segbits >> (rr * VEC) & 1u);
             const uint32_t kill = S >> 1;   // lane t+1 starts an instance: no carry out of lane t
 #pragma unroll
             for (int c = 0; c < NCH; c++) {
@@ -197,11 +243,9 @@ addsub_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t m, uint6
         }
 
         // ---- replay rows with the resolved carries
-        uint32_t lastbits = 0;   // SUB: bit (rr*VEC+e): a-b borrow out of a limb that ends an instance
+        uint32_t c1bits = 0, c2bits = 0;   // sub: borrow into each limb for a-b and b-a
 #pragma unroll
         for (int rr = 0; rr < ROWS; rr++) {
-            const int vi = (int)((warp * ROWS + rr) * 32 + lane);
-            const int li0 = vi * VEC - off;
             uint32_t c_in[NCH];
 #pragma unroll
             for (int c = 0; c < NCH; c++) {
@@ -212,33 +256,30 @@ addsub_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t m, uint6
             }
 #pragma unroll
             for (int e = 0; e < VEC; e++) {
-                const int li = li0 + e;
-                const bool ok = li >= 0 && li < len;
-                const uint32_t q = ok ? mdiv.div((uint32_t)li) : 0u;
-                const int pos = li - (int)(q * m);
-                const bool seg = ok && pos == 0;
-                const T x = av[rr][e], y = bv[rr][e];
+                const int bit = rr * VEC + e;
+                const uint32_t seg = (segbits >> bit) & 1u;
+                const uint32_t g0 = (gbits >> bit) & 1u;
                 if (OP == OP_ADD) {
                     if (e > 0 && seg) c_in[0] = 0;
-                    const T s = x + y;
-                    const uint32_t g = s < x, p = s == HI;
-                    av[rr][e] = s + (T)c_in[0];
-                    c_in[0] = g | (p & c_in[0]);
+                    const uint32_t p = d[rr][e] == HI;
+                    const T s = d[rr][e];
+                    d[rr][e] = s + (T)c_in[0];
+                    c_in[0] = g0 | (p & c_in[0]);
                 } else {
                     if (e > 0 && seg) { c_in[0] = 0; c_in[1] = 0; }
-                    const uint32_t g0 = x < y, g1 = y < x, p = x == y;
-                    av[rr][e] = x - y - (T)c_in[0];
-                    bv[rr][e] = y - x - (T)c_in[1];
+                    const uint32_t p = d[rr][e] == 0;
+                    c1bits |= c_in[0] << bit;
+                    c2bits |= c_in[1] << bit;
                     c_in[0] = g0 | (p & c_in[0]);
-                    c_in[1] = g1 | (p & c_in[1]);
-                    if (ok && pos == (int)m - 1) {
-                        s_sign[q] = (uint8_t)c_in[0];
-                        lastbits |= 1u << (rr * VEC + e);
+                    c_in[1] = (~g0 & ~p & 1u) | (p & c_in[1]);
+                    if ((lastbits >> bit) & 1u) {
+                        // instance index of this limb within the tile
+                        const int li = ((int)((warp * ROWS + rr) * 32 + lane)) * VEC - off + e;
+                        s_sign[mdiv.div((uint32_t)li)] = (uint8_t)c_in[0];
                     }
                 }
             }
         }
-        (void)lastbits;
 
         if (OP == OP_SUB) __syncthreads();
 
@@ -249,17 +290,25 @@ addsub_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t m, uint6
             const int li0 = vi * VEC - off;
             const uint64_t gi = abase + (uint64_t)vi * VEC;
             T out[VEC];
+            if (OP == OP_ADD) {
 #pragma unroll
-            for (int e = 0; e < VEC; e++) {
-                if (OP == OP_ADD) {
-                    out[e] = av[rr][e];
-                } else {
-                    const int li = li0 + e;
-                    const bool ok = li >= 0 && li < len;
-                    const uint32_t q = ok ? mdiv.div((uint32_t)li) : 0u;
+                for (int e = 0; e < VEC; e++) out[e] = d[rr][e];
+            } else {
+                uint32_t q = 0;
+                const uint32_t rowvalid = (validbits >> (rr * VEC)) & ((1u << VEC) - 1u);
+                if (rowvalid) {
+                    const int lfirst = li0 + (int)(__ffs(rowvalid) - 1);
+                    q = mdiv.div((uint32_t)lfirst);
+                }
+#pragma unroll
+                for (int e = 0; e < VEC; e++) {
+                    const int bit = rr * VEC + e;
+                    const bool ok = (validbits >> bit) & 1u;
+                    if (e > 0 && ((segbits >> bit) & 1u) && ((validbits >> (bit - 1)) & 1u)) q++;
                     const bool neg = ok && s_sign[q];
-                    out[e] = neg ? bv[rr][e] : av[rr][e];
-                    if (ok && sign_out != nullptr && li == (int)(q * m)) sign_out[inst0 + q] = s_sign[q];
+                    const T c1 = (T)((c1bits >> bit) & 1u), c2 = (T)((c2bits >> bit) & 1u);
+                    out[e] = neg ? (T)(0 - d[rr][e] - c2) : (T)(d[rr][e] - c1);
+                    if (ok && sign_out != nullptr && ((segbits >> bit) & 1u)) sign_out[inst0 + q] = s_sign[q];
                 }
             }
             if (li0 >= 0 && li0 + VEC <= len) {
