@@ -29,8 +29,8 @@ template <typename T, int VEC>
 __device__ __forceinline__ void load_limbs(const T* p, T (&v)[VEC]) {
     if constexpr (VEC * sizeof(T) == 16) {
         uint4 x;
-        asm volatile("ld.global.cs.v4.u32 {%0,%1,%2,%3}, [%4];"
-                     : "=r"(x.x), "=r"(x.y), "=r"(x.z), "=r"(x.w) : "l"(p));
+        asm("ld.global.cs.v4.u32 {%0,%1,%2,%3}, [%4];"
+            : "=r"(x.x), "=r"(x.y), "=r"(x.z), "=r"(x.w) : "l"(p));
         if constexpr (sizeof(T) == 8) {
             v[0] = ((uint64_t)x.y << 32) | x.x;
             v[1] = ((uint64_t)x.w << 32) | x.z;
@@ -137,32 +137,38 @@ addsub_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t m, uint6
 
         // d = a + b (add) or a - b (sub), both without carries; gbits = carry
         // (borrow) generated by each limb on its own
-        T d[ROWS][VEC];
+        T d[ROWS][VEC], y[ROWS][VEC];
         uint32_t gbits = 0, segbits = 0, lastbits = 0, validbits = 0;
 
+        // issue every load of the tile before using any of them
 #pragma unroll
         for (int rr = 0; rr < ROWS; rr++) {
             const int vi = (int)((warp * ROWS + rr) * 32 + lane);
             const int li0 = vi * VEC - off;
             const uint64_t gi = abase + (uint64_t)vi * VEC;
-            T x[VEC], y[VEC];
             if (li0 >= 0 && li0 + VEC <= len) {
-                load_limbs<T, VEC>(a + gi, x);
-                load_limbs<T, VEC>(b + gi, y);
+                load_limbs<T, VEC>(a + gi, d[rr]);
+                load_limbs<T, VEC>(b + gi, y[rr]);
             } else {
 #pragma unroll
                 for (int e = 0; e < VEC; e++) {
                     const int li = li0 + e;
                     const bool ok = li >= 0 && li < len;
-                    x[e] = ok ? __ldcs(a + gi + e) : (T)0;
-                    y[e] = ok ? __ldcs(b + gi + e) : (T)0;
+                    d[rr][e] = ok ? __ldcs(a + gi + e) : (T)0;
+                    y[rr][e] = ok ? __ldcs(b + gi + e) : (T)0;
                 }
             }
+        }
+#pragma unroll
+        for (int rr = 0; rr < ROWS; rr++) {
+            const int vi = (int)((warp * ROWS + rr) * 32 + lane);
+            const int li0 = vi * VEC - off;
 #pragma unroll
             for (int e = 0; e < VEC; e++) {
+                const T x = d[rr][e];
                 uint32_t g;
-                if (OP == OP_ADD) { d[rr][e] = x[e] + y[e]; g = d[rr][e] < x[e]; }
-                else              { d[rr][e] = x[e] - y[e]; g = x[e] < y[e]; }
+                if (OP == OP_ADD) { d[rr][e] = x + y[rr][e]; g = d[rr][e] < x; }
+                else              { d[rr][e] = x - y[rr][e]; g = x < y[rr][e]; }
                 gbits |= g << (rr * VEC + e);
             }
             uint32_t sg, la, va, q0, wr;
