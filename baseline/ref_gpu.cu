@@ -1,0 +1,86 @@
+// ref_gpu.cu -- launches the reference's own CUDA kernels (tossenxD/big-int,
+// cuda/ker-add.cu.h and cuda/ker-mul.cu.h, unmodified) as a GPU baseline on
+// the same device pointers the library uses.  The headers are staged into
+// baseline/_ref/cuda by install_ref.sh and this file is compiled on the GPU
+// box into baseline/_ref/libref_gpu.so.  Nothing here is part of the library.
+//
+// Launch geometry follows the reference's host wrappers exactly:
+//   gpuAdd (cuda/main.cu:130-135):      q = m/4 <= 1024 ? 4 : ceil(m/1024),
+//                                       ipb = ceil(256/(m/q)), block = ipb*m/q,
+//                                       grid = n/ipb, kernel baddKer3<Base,m,q,ipb>
+//   gpuMultiply (cuda/main.cu:302-307): q = 4, ipb = ceil(128/(m/4)),
+//                                       block = ipb*m/4, grid = n/ipb,
+//                                       kernel convMul5<Base,m,ipb>
+// As in the reference, grid = n/ipb drops a remainder of instances, so
+// callers pass n divisible by ipb.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "ker-add.cu.h"
+#include "ker-mul.cu.h"
+
+template <class Base, uint32_t m>
+static int launch_add(const void* a, const void* b, void* r, uint32_t n, cudaStream_t s) {
+    constexpr uint32_t q = (m / 4 <= 1024) ? 4 : (m + 1024 - 1) / 1024;
+    constexpr uint32_t ipb = (256 + m / q - 1) / (m / q);
+    using uint_t = typename Base::uint_t;
+    if (n % ipb) return 2;
+    baddKer3<Base, m, q, ipb><<<n / ipb, ipb * (m / q), 0, s>>>((uint_t*)a, (uint_t*)b, (uint_t*)r);
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
+
+template <class Base, uint32_t m>
+static int launch_mul(const void* a, const void* b, void* r, uint32_t n, cudaStream_t s) {
+    constexpr uint32_t q = 4;
+    constexpr uint32_t ipb = (128 + (m / q) - 1) / (m / q);
+    using uint_t = typename Base::uint_t;
+    if (n % ipb) return 2;
+    convMul5<Base, m, ipb><<<n / ipb, ipb * (m / q), 0, s>>>((uint_t*)a, (uint_t*)b, (uint_t*)r);
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
+
+extern "C" {
+
+// r = (a + b) mod B^m with the reference's best addition kernel (C-V3).
+int ref_add_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (m) {
+    case 16: return launch_add<U64bits, 16>(a, b, r, n, s);
+    case 32: return launch_add<U64bits, 32>(a, b, r, n, s);
+    case 64: return launch_add<U64bits, 64>(a, b, r, n, s);
+    case 128: return launch_add<U64bits, 128>(a, b, r, n, s);
+    case 256: return launch_add<U64bits, 256>(a, b, r, n, s);
+    case 512: return launch_add<U64bits, 512>(a, b, r, n, s);
+    case 1024: return launch_add<U64bits, 1024>(a, b, r, n, s);
+    case 2048: return launch_add<U64bits, 2048>(a, b, r, n, s);
+    case 4096: return launch_add<U64bits, 4096>(a, b, r, n, s);
+    default: return 1;
+    }
+}
+
+// r = (a * b) mod B^m with the reference's best multiplication kernel (C-V5);
+// the full product of m-limb inputs is this call at size 2m on zero-padded
+// inputs.
+int ref_mul_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (m) {
+    case 64: return launch_mul<U64bits, 64>(a, b, r, n, s);
+    case 128: return launch_mul<U64bits, 128>(a, b, r, n, s);
+    case 256: return launch_mul<U64bits, 256>(a, b, r, n, s);
+    case 512: return launch_mul<U64bits, 512>(a, b, r, n, s);
+    case 1024: return launch_mul<U64bits, 1024>(a, b, r, n, s);
+    case 2048: return launch_mul<U64bits, 2048>(a, b, r, n, s);
+    default: return 1;
+    }
+}
+
+int ref_mul_u32(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (m) {
+    case 64: return launch_mul<U32bits, 64>(a, b, r, n, s);
+    case 128: return launch_mul<U32bits, 128>(a, b, r, n, s);
+    default: return 1;
+    }
+}
+
+}  // extern "C"

@@ -287,8 +287,72 @@ def measure_extra(B, L, stream, args):
         div[f"m{mv}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4)}
         del u, v, q, rr, st
     out["div_u64_2m_by_m"] = div
+    out["reference_cuda_kernels"] = measure_reference_kernels(B, L, stream)
     torch.cuda.empty_cache()
     return out
+
+
+def measure_reference_kernels(B, L, stream):
+    """The reference's own kernels (baddKer3, convMul5) on the same GPU and inputs."""
+    import torch
+
+    from bigint_gb300.workloads import MUL_U64, addsub_u64_device, mul2048_u32, mul_u64_device
+
+    sys.path.insert(0, os.path.join(REPO, "baseline"))
+    try:
+        import refgpu
+
+        if not refgpu.build() or refgpu.lib() is None:
+            return {"unavailable": "reference kernel headers were not staged"}
+    except Exception as e:  # a baseline only: never fail the bench on it
+        return {"unavailable": f"reference kernels did not build: {e}"}
+    R = refgpu.lib()
+    sp = int(stream.cuda_stream)
+    res = {"add_u64_gbs": {}, "mul_u64": {}}
+    total = 1 << 27
+    for bits in BITS:
+        m = bits // 64
+        a, b = addsub_u64_device(bits, seed=SEED_ADDSUB, total_limbs=total, op="add")
+        n = a.shape[0]
+        r = torch.empty_like(a)
+        ms_ref = event_time(stream, lambda: R.ref_add_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, sp), 5)
+        ms_ours = event_time(stream, lambda: check(L, L.bi_add_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, sp)), 5)
+        res["add_u64_gbs"][str(bits)] = {"reference_baddKer3": round(3 * total * 8 / ms_ref / 1e6, 1),
+                                          "ours": round(3 * total * 8 / ms_ours / 1e6, 1)}
+        del a, b, r
+    for m, n in MUL_U64:
+        a, b = mul_u64_device(m, n)
+        rt = torch.empty_like(a)
+        ms_tr = event_time(stream, lambda: R.ref_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, sp), 3)
+        ms_ours_tr = event_time(stream, lambda: check(L, L.bi_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, sp)), 3)
+        entry = {"truncated_reference_inst_per_s": round(n / ms_tr * 1e3),
+                 "truncated_ours_inst_per_s": round(n / ms_ours_tr * 1e3)}
+        if 2 * m in refgpu.MUL_SIZES_U64:
+            pa = torch.zeros((n, 2 * m), dtype=torch.int64, device="cuda")
+            pb = torch.zeros_like(pa)
+            pa[:, :m] = a
+            pb[:, :m] = b
+            rf = torch.empty_like(pa)
+            ms_f = event_time(stream, lambda: R.ref_mul_u64(pa.data_ptr(), pb.data_ptr(), rf.data_ptr(), 2 * m, n, sp), 3)
+            ms_ours_f = event_time(stream, lambda: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), rf.data_ptr(), m, n, sp)), 3)
+            entry["full_reference_inst_per_s"] = round(n / ms_f * 1e3)
+            entry["full_ours_inst_per_s"] = round(n / ms_ours_f * 1e3)
+            del pa, pb, rf
+        else:
+            entry["full_reference"] = "unavailable: convMul5 at 2m=%d limbs needs >48 KiB static shared memory" % (2 * m)
+        res["mul_u64"][f"m{m}_n{n}"] = entry
+        del a, b, rt
+    a, b = mul2048_u32()
+    n, m = a.shape
+    pa = np.zeros((n, 2 * m), np.uint32)
+    pb = np.zeros((n, 2 * m), np.uint32)
+    pa[:, :m] = a
+    pb[:, :m] = b
+    dpa, dpb = B.to_device(pa), B.to_device(pb)
+    rf = torch.empty_like(dpa)
+    ms_ref = event_time(stream, lambda: R.ref_mul_u32(dpa.data_ptr(), dpb.data_ptr(), rf.data_ptr(), 2 * m, n, sp), 20)
+    res["mul2048_u32_full_reference_inst_per_s"] = round(n / ms_ref * 1e3)
+    return res
 
 
 def run_single(args) -> None:

@@ -117,6 +117,41 @@ static bi_status host_pipelined(const HostIO& io, uint64_t n, Launch launch) {
     return rs;
 }
 
+// Device-accessible alias of a pinned (page-locked, registered) host
+// buffer, or nullptr for pageable memory.
+static void* pinned_alias(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+    return at.devicePointer;
+}
+
+// When every host buffer is pinned, the kernel reads and writes them in
+// place over the CPU-GPU link (one pass, no staging copies): the link is the
+// bound, and a bandwidth-bound kernel keeps it fuller than chunked copies.
+template <typename Launch>
+static bool run_in_place(const HostIO& io, uint64_t n, Launch launch, bi_status* rs) {
+    void* d[5] = {};
+    for (int j = 0; j < 2; j++)
+        if (io.in_bytes[j] && !(d[j] = pinned_alias(io.in[j]))) return false;
+    for (int j = 0; j < 3; j++)
+        if (io.out_bytes[j] && io.out[j] && !(d[2 + j] = pinned_alias(io.out[j]))) return false;
+    cudaStream_t st;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    *rs = launch(d[0], d[1], d[2], d[3], (uint8_t*)d[4], n, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (*rs == BI_OK && e != cudaSuccess) *rs = cuda_ok(e, "in-place host launch");
+    cudaStreamDestroy(st);
+    return true;
+}
+
 template <typename T, typename Launch>
 static bi_status host_binary(const T* ha, const T* hb, T* hr, uint8_t* hsign, uint32_t m, uint64_t n,
                              size_t out_limbs_per_inst, Launch launch) {
@@ -128,9 +163,12 @@ static bi_status host_binary(const T* ha, const T* hb, T* hr, uint8_t* hsign, ui
     io.in[1] = hb; io.in_bytes[1] = (size_t)m * sizeof(T);
     io.out[0] = hr; io.out_bytes[0] = out_limbs_per_inst * sizeof(T);
     io.out[2] = hsign; io.out_bytes[2] = hsign ? 1 : 0;
-    return host_pipelined(io, n, [&](void* da, void* db, void* dr, void*, uint8_t* ds, uint64_t cnt, cudaStream_t s) {
+    auto fn = [&](void* da, void* db, void* dr, void*, uint8_t* ds, uint64_t cnt, cudaStream_t s) {
         return launch((const T*)da, (const T*)db, (T*)dr, ds, cnt, s);
-    });
+    };
+    bi_status rs;
+    if (run_in_place(io, n, fn, &rs)) return rs;
+    return host_pipelined(io, n, fn);
 }
 
 template <typename T>
@@ -152,13 +190,14 @@ static bi_status host_div(const T* hu, const T* hv, T* hq, T* hr, uint8_t* hstat
     io.out[0] = hq; io.out_bytes[0] = (size_t)mu * sizeof(T);
     io.out[1] = hr; io.out_bytes[1] = (size_t)mv * sizeof(T);
     io.out[2] = stat; io.out_bytes[2] = 1;
-    bi_status rs = host_pipelined(io, n, [&](void* du, void* dv, void* dq, void* dr, uint8_t* ds, uint64_t cnt,
-                                             cudaStream_t s) {
+    auto fn = [&](void* du, void* dv, void* dq, void* dr, uint8_t* ds, uint64_t cnt, cudaStream_t s) {
         if constexpr (sizeof(T) == 8)
             return bi_div_u64((const T*)du, (const T*)dv, (T*)dq, (T*)dr, ds, mu, mv, cnt, s);
         else
             return bi_div_u32((const T*)du, (const T*)dv, (T*)dq, (T*)dr, ds, mu, mv, cnt, s);
-    });
+    };
+    bi_status rs;
+    if (!run_in_place(io, n, fn, &rs)) rs = host_pipelined(io, n, fn);
     if (rs == BI_OK) {
         for (uint64_t i = 0; i < n; i++) {
             if (stat[i] == 1) { rs = set_error(BI_EDIV0, "instance %llu has a zero divisor", (unsigned long long)i); break; }

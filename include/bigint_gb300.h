@@ -15,9 +15,11 @@
  *     stream-ordered, and they allocate no memory;
  *   - host entry points (bi_host_*) take host pointers and return when the
  *     results are back in host memory -- the shape of the reference's
- *     gpuAdd/gpuMultiply wrappers; internally the batch is cut into chunks
- *     whose copies in, kernels and copies out overlap on three streams
- *     (pinned host buffers get the full link bandwidth);
+ *     gpuAdd/gpuMultiply wrappers.  If every host buffer of the call is
+ *     pinned (cudaHostAlloc / cudaHostRegister), the kernel reads and writes
+ *     them in place over the CPU-GPU link; otherwise the batch is cut into
+ *     chunks whose copies in, kernels and copies out overlap on three
+ *     streams;
  *   - n == 0 is a no-op; m == 0 or a NULL buffer with n > 0 is BI_EINVAL;
  *   - any n is accepted: unlike the reference launch (grid = n/ipb, which
  *     drops the remainder, cuda/main.cu:135,307) every instance is computed;

@@ -168,3 +168,25 @@ def test_full_size_sweep(bigint, oracle, bits):
             assert (sign[idx].cpu().numpy() == s_ref).all()
         del a, b, r
         torch.cuda.empty_cache()
+
+
+def test_host_entry_in_place_on_pinned_buffers(bigint, oracle):
+    """Pinned host buffers take the in-place path (kernel reads host memory)."""
+    import ctypes
+
+    import torch
+
+    B = bigint
+    L = B.lib()
+    n, m = 1000, 33
+    a = uniform_limbs(71, n, m)
+    b = uniform_limbs(72, n, m)
+    ha = torch.from_numpy(a.view(np.int64)).pin_memory()
+    hb = torch.from_numpy(b.view(np.int64)).pin_memory()
+    hr = torch.empty_like(ha).pin_memory()
+    hs = torch.empty(n, dtype=torch.uint8).pin_memory()
+    assert L.bi_host_add_u64(ha.data_ptr(), hb.data_ptr(), hr.data_ptr(), m, n) == 0
+    assert (hr.numpy().view(np.uint64) == oracle.add(a, b)).all()
+    assert L.bi_host_sub_u64(ha.data_ptr(), hb.data_ptr(), hr.data_ptr(), hs.data_ptr(), m, n) == 0
+    r_ref, s_ref = oracle.sub(a, b)
+    assert (hr.numpy().view(np.uint64) == r_ref).all() and (hs.numpy() == s_ref).all()
