@@ -101,6 +101,12 @@ SIGNATURES: dict[str, list] = {
     "bi_host_div_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64],
     "bi_max_limbs_div_u64": [],
     "bi_max_limbs_div_u32": [],
+    "bi_plan_create": [_P, _P, _U64],
+    "bi_plan_execute": [_P, _P, _P, _P, _P],
+    "bi_plan_autotune": [_P, _P, _P, _P, _I, _P],
+    "bi_plan_set_tuning": [_P, _I, _I, _I],
+    "bi_plan_stats": [_P, _P],
+    "bi_plan_destroy": [_P],
     "bi_probe_intpipe": [_P, _P],
 }
 _RESTYPE = {
@@ -247,6 +253,57 @@ def probe_intpipe(stream=None) -> dict:
     rates = (ctypes.c_double * 6)()
     _check(lib().bi_probe_intpipe(ctypes.cast(rates, ctypes.c_void_p), _stream_ptr(stream)))
     return dict(zip(PROBE_FORMS, list(rates)))
+
+
+# ---------------------------------------------------------------------------
+# uneven batches (include/bigint_gb300.h: bi_desc, bi_plan_*)
+# ---------------------------------------------------------------------------
+
+OP_ADD, OP_SUB, OP_MUL, OP_MULFULL, OP_DIV = 0, 1, 2, 3, 4
+
+DESC_DTYPE = np.dtype([("op", "<u4"), ("m", "<u4"), ("mb", "<u4"), ("reserved", "<u4"),
+                       ("a", "<u8"), ("b", "<u8"), ("r", "<u8"), ("r2", "<u8"), ("flag", "<u8")])
+
+
+class Plan:
+    """A bucketed, graph-captured execution plan for an uneven batch."""
+
+    def __init__(self, descs: np.ndarray):
+        descs = np.ascontiguousarray(descs, dtype=DESC_DTYPE)
+        self.count = len(descs)
+        self._h = ctypes.c_void_p()
+        _check(lib().bi_plan_create(ctypes.byref(self._h), descs.ctypes.data_as(ctypes.c_void_p), self.count))
+
+    def execute(self, arena_in, arena_out, flags=None, stream=None):
+        _check(lib().bi_plan_execute(self._h, arena_in.data_ptr(), arena_out.data_ptr(),
+                                     flags.data_ptr() if flags is not None else None, _stream_ptr(stream)))
+
+    def autotune(self, arena_in, arena_out, flags=None, reps: int = 3):
+        chosen = (ctypes.c_int * 3)()
+        _check(lib().bi_plan_autotune(self._h, arena_in.data_ptr(), arena_out.data_ptr(),
+                                      flags.data_ptr() if flags is not None else None, reps,
+                                      ctypes.cast(chosen, ctypes.c_void_p)))
+        return {"addsub_rows": chosen[0], "addsub_limbs_per_lane_row": chosen[1], "mul_ipc_divisor": chosen[2]}
+
+    def set_tuning(self, rows: int, vec: int, ipc_div: int):
+        _check(lib().bi_plan_set_tuning(self._h, rows, vec, ipc_div))
+
+    def stats(self) -> dict:
+        st = (ctypes.c_uint64 * 6)()
+        _check(lib().bi_plan_stats(self._h, ctypes.cast(st, ctypes.c_void_p)))
+        keys = ("addsub", "mul", "mul_items", "div", "mul_smem_bytes", "div_smem_bytes")
+        return dict(zip(keys, list(st)))
+
+    def close(self):
+        if self._h:
+            lib().bi_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 # ---------------------------------------------------------------------------

@@ -12,6 +12,10 @@ any machine.  Seeds are 1000 + the workload index:
                     odd; sub: a low run of zero limbs, b = 1).
   * mul_u64      -- u64 limbs, m in {64, 256, 1024, 2048}, n in
                     {2^16, 2^14, 2^12, 2^11}, uniform; full 2m-limb product.
+  * uneven_batch -- 100k instances, sizes log-uniform over 256..65536 bits
+                    (u64 limbs), ops 20 % add, 20 % sub, 40 % full multiply,
+                    20 % division (dividend 2m limbs, divisor m limbs with a
+                    nonzero top limb); seed 1003.
 """
 from __future__ import annotations
 
@@ -144,3 +148,46 @@ def addsub_u64_device(bits: int, seed: int = 1001, total_limbs: int = 1 << 27, o
 def mul_u64_device(m: int, n: int, seed: int = 1002, device="cuda"):
     return (device_uniform_u64(seed, n, m, device=device),
             device_uniform_u64(seed, n, m, offset=n * m, device=device))
+
+
+def uneven_batch(n: int = 100_000, seed: int = 1003, min_bits: int = 256, max_bits: int = 65536):
+    """Descriptors and input arena of the uneven-size batch.
+
+    Returns (descs, arena_in, out_limbs, flag_bytes): descs is a DESC_DTYPE
+    array, arena_in a uint64 array holding every operand back to back in
+    descriptor order; outputs go to an arena of out_limbs limbs (per
+    instance: m for add/sub, 2m for the full product, 2m quotient + m
+    remainder for division) and a flag arena of flag_bytes bytes.
+    """
+    from . import DESC_DTYPE, OP_ADD, OP_DIV, OP_MULFULL, OP_SUB
+
+    u = (splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+    lo, hi = np.log2(min_bits), np.log2(max_bits)
+    bits = np.exp2(lo + (hi - lo) * u)
+    m = np.maximum(1, np.ceil(bits / 64.0)).astype(np.int64)
+    sel = (splitmix64(seed + 1, n) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+    op = np.where(sel < 0.2, OP_ADD, np.where(sel < 0.4, OP_SUB, np.where(sel < 0.8, OP_MULFULL, OP_DIV)))
+    ma = np.where(op == OP_DIV, 2 * m, m)           # first operand limbs
+    mb = m                                          # second operand limbs
+    a_off = np.zeros(n, np.int64)
+    a_off[1:] = np.cumsum(ma + mb)[:-1]
+    b_off = a_off + ma
+    rl = np.where(op == OP_ADD, m, np.where(op == OP_SUB, m, 2 * m))   # q has the dividend's 2m limbs
+    r2l = np.where(op == OP_DIV, m, 0)
+    r_off = np.zeros(n, np.int64)
+    r_off[1:] = np.cumsum(rl + r2l)[:-1]
+    total_in = int((ma + mb).sum())
+    arena = splitmix64(seed + 2, total_in)
+    div_idx = np.nonzero(op == OP_DIV)[0]
+    top = b_off[div_idx] + mb[div_idx] - 1          # divisor top limb nonzero
+    arena[top] |= np.uint64(1)
+    d = np.zeros(n, dtype=DESC_DTYPE)
+    d["op"] = op
+    d["m"] = ma
+    d["mb"] = mb
+    d["a"] = a_off
+    d["b"] = b_off
+    d["r"] = r_off
+    d["r2"] = r_off + rl
+    d["flag"] = np.arange(n)
+    return d, arena, int((rl + r2l).sum()), n

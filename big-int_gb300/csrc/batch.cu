@@ -1,0 +1,647 @@
+// batch.cu -- uneven batches: instances of different operations and sizes in
+// one graph-captured launch.
+//
+// The reference launches one kernel per (operation, size) with the size a
+// template parameter (cuda/main.cu:476-515), so a batch of mixed sizes costs
+// one launch per distinct size.  Here a plan groups the descriptors once:
+//   * add/sub instances, largest first, go to a persistent kernel in which
+//     each warp takes one instance at a time (warp_addsub: rows of 32 lanes x
+//     16 bytes, carries resolved by ballots, a subtraction first finds the
+//     larger operand from the top limb down as the reference's bsub does,
+//     futhark/sub.fut:14-16) -- no shared memory and no CTA barrier, so any
+//     size mix keeps the warps busy;
+//   * multiplications are bucketed by padded size; a persistent CTA takes a
+//     bucket item (as many instances as fit one CTA, mulcore.cuh);
+//   * divisions, most expensive first, go one per CTA to a persistent kernel
+//     (divcore.cuh).
+// The three persistent kernels run concurrently on forked streams; the fork,
+// the three launches, the counter reset and the join are captured once into a
+// CUDA graph and replayed by every bi_plan_execute.  Work is handed out with
+// one atomic counter per kernel (no waiting on other CTAs).
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "divcore.cuh"
+#include "mulcore.cuh"
+
+namespace bi {
+
+constexpr uint32_t BATCH_MAX_LIMBS = 2048;   // per operand (64-bit limbs)
+
+struct MulItem {
+    uint32_t first;   // index into the mul list
+    uint32_t count;   // instances in this item
+    uint32_t Lp;      // padded limbs (geometry)
+    uint32_t full;    // 1 = full product, 0 = truncated
+};
+
+struct BatchTune {
+    int addsub_rows;   // rows of 32 lanes loaded per step (limbs per lane = rows * VEC)
+    int addsub_vec;    // limbs per lane per row: 2 (16-byte accesses) or 1
+    int mul_ipc_div;   // divide the default instances-per-CTA by this
+};
+
+// ---------------------------------------------------------------------------
+// warp-per-instance add / sign-magnitude subtraction
+// ---------------------------------------------------------------------------
+template <int VEC>
+__device__ __forceinline__ void ld_row(const uint64_t* p, int64_t base, uint32_t m, uint64_t (&v)[VEC]) {
+    if (VEC == 2 && base >= 0 && base + 2 <= (int64_t)m) {
+        const ulonglong2 x = __ldcs(reinterpret_cast<const ulonglong2*>(p + base));
+        v[0] = x.x;
+        if constexpr (VEC == 2) v[1] = x.y;
+    } else {
+#pragma unroll
+        for (int e = 0; e < VEC; e++) v[e] = (base + e >= 0 && base + e < (int64_t)m) ? __ldcs(p + base + e) : 0;
+    }
+}
+
+template <int VEC, int R>
+__device__ void warp_addsub(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* sign, uint32_t m,
+                            bool sub) {
+    constexpr int ROWL = 32 * VEC;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nrows = (m + ROWL - 1) / ROWL;
+    if (sub) {
+        // which operand is larger: scan rows from the most significant end
+        bool lt = false;
+        for (int row = (int)nrows - 1; row >= 0; row--) {
+            const int64_t base = (int64_t)row * ROWL + lane * VEC;
+            uint64_t x[VEC], y[VEC];
+            ld_row<VEC>(a, base, m, x);
+            ld_row<VEC>(b, base, m, y);
+            int top = -1;
+            bool lane_lt = false;
+#pragma unroll
+            for (int e = 0; e < VEC; e++)
+                if (x[e] != y[e]) { top = e; lane_lt = x[e] < y[e]; }
+            const uint32_t diff = __ballot_sync(0xffffffffu, top >= 0);
+            if (diff) {
+                const int hi = 31 - __clz(diff);
+                lt = __shfl_sync(0xffffffffu, lane_lt, hi);
+                break;
+            }
+        }
+        if (lt) {   // |a - b| = b - a
+            const uint64_t* t = a;
+            a = b;
+            b = t;
+        }
+        if (lane == 0 && sign) *sign = lt ? 1 : 0;
+    }
+    uint32_t cin = 0;
+    for (uint32_t row0 = 0; row0 < nrows; row0 += R) {
+        uint64_t x[R][VEC], y[R][VEC];
+#pragma unroll
+        for (int rr = 0; rr < R; rr++) {
+            const int64_t base = (int64_t)(row0 + rr) * ROWL + lane * VEC;
+            ld_row<VEC>(a, base, m, x[rr]);
+            ld_row<VEC>(b, base, m, y[rr]);
+        }
+#pragma unroll
+        for (int rr = 0; rr < R; rr++) {
+            if (row0 + rr >= nrows) break;
+            uint64_t s[VEC];
+            uint32_t G = 0, P = 1, gb = 0, pb = 0;
+#pragma unroll
+            for (int e = 0; e < VEC; e++) {
+                uint32_t g, p;
+                if (!sub) { s[e] = x[rr][e] + y[rr][e]; g = s[e] < x[rr][e]; p = s[e] == ~0ull; }
+                else      { s[e] = x[rr][e] - y[rr][e]; g = x[rr][e] < y[rr][e]; p = x[rr][e] == y[rr][e]; }
+                gb |= g << e;
+                pb |= p << e;
+                G = g | (p & G);
+                P = p & P;
+            }
+            const uint32_t A = __ballot_sync(0xffffffffu, G | P);
+            const uint32_t B = __ballot_sync(0xffffffffu, G);
+            const WarpCarry wc = warp_carry_resolve(A, B, cin);
+            uint32_t c = (wc.carries >> lane) & 1u;
+            cin = wc.cout;
+            const int64_t base = (int64_t)(row0 + rr) * ROWL + lane * VEC;
+            uint64_t out[VEC];
+#pragma unroll
+            for (int e = 0; e < VEC; e++) {
+                out[e] = sub ? s[e] - c : s[e] + c;
+                c = ((gb >> e) & 1u) | (((pb >> e) & 1u) & c);
+            }
+            if (VEC == 2 && base + 2 <= (int64_t)m) {
+                ulonglong2 v;
+                v.x = out[0];
+                v.y = out[VEC - 1];
+                __stcs(reinterpret_cast<ulonglong2*>(r + base), v);
+            } else {
+#pragma unroll
+                for (int e = 0; e < VEC; e++)
+                    if (base + e < (int64_t)m) __stcs(r + base + e, out[e]);
+            }
+        }
+    }
+}
+
+template <int VEC, int R>
+__global__ void __launch_bounds__(256)
+batch_addsub_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                    uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(counter, 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= count) break;
+        const bi_desc d = descs[list[idx]];
+        const bool sub = d.op == BI_OP_SUB;
+        uint8_t* sg = (sub && flags) ? flags + d.flag : nullptr;
+        // 16-byte accesses need even limb offsets (the arenas are 16-byte aligned)
+        if (VEC == 2 && ((d.a | d.b | d.r) & 1ull) == 0)
+            warp_addsub<VEC, R>(in + d.a, in + d.b, out + d.r, sg, d.m, sub);
+        else
+            warp_addsub<1, R>(in + d.a, in + d.b, out + d.r, sg, d.m, sub);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// persistent multiply and divide kernels
+// ---------------------------------------------------------------------------
+constexpr int BATCH_CTA = 256;
+
+__global__ void __launch_bounds__(BATCH_CTA, 2)
+batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list,
+                 const MulItem* __restrict__ items, uint32_t nitems, uint32_t* counter, const uint64_t* in,
+                 uint64_t* out, int ipc_div) {
+    extern __shared__ __align__(16) uint64_t smem[];
+    __shared__ uint32_t s_item;
+    __shared__ uint64_t s_a[BATCH_CTA], s_b[BATCH_CTA], s_r[BATCH_CTA];
+    __shared__ uint32_t s_m[BATCH_CTA];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t it = s_item;
+        if (it >= nitems) break;
+        const MulItem item = items[it];
+        for (uint32_t i = threadIdx.x; i < item.count; i += blockDim.x) {
+            const bi_desc& d = descs[list[item.first + i]];
+            s_a[i] = d.a;
+            s_b[i] = d.b;
+            s_r[i] = d.r;
+            s_m[i] = d.m;
+        }
+        uint32_t cap = item.count;
+        const MulGeom g0 = mul_geometry(item.Lp, item.full != 0, cap);
+        const MulGeom g = ipc_div > 1 && g0.ipc > 1 ? mul_geometry(item.Lp, item.full != 0, (g0.ipc + ipc_div - 1) / ipc_div)
+                                                    : g0;
+        __syncthreads();
+        uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + (size_t)g.ipc * g.IS);
+        const FastDiv lpdiv(g.Lp);
+        const uint32_t full = item.full;
+        // the item's instances in rounds of g.ipc
+        for (uint32_t base = 0; base < item.count; base += g.ipc) {
+            auto load = [&](uint32_t li, uint32_t x, uint64_t& va, uint64_t& vb) {
+                const uint32_t k = base + li;
+                if (k >= item.count || x >= s_m[k]) return;
+                va = in[s_a[k] + x];
+                vb = in[s_b[k] + x];
+            };
+            auto store = [&](uint32_t li, uint32_t x, uint64_t v) {
+                const uint32_t k = base + li;
+                if (k >= item.count) return;
+                if (x < (full ? 2 * s_m[k] : s_m[k])) out[s_r[k] + x] = v;
+            };
+            mul_cta<MUL_C>(g, smem, scratch, lpdiv, load, store);
+        }
+        __syncthreads();   // s_item and the descriptor cache are rewritten next round
+    }
+}
+
+__global__ void __launch_bounds__(BATCH_CTA, 2)
+batch_div_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                 uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    extern __shared__ __align__(16) uint64_t smem[];
+    __shared__ uint32_t s_idx;
+    for (;;) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t idx = s_idx;
+        __syncthreads();
+        if (idx >= count) break;
+        const bi_desc d = descs[list[idx]];
+        const DivGeom g = div_geom(d.m, d.mb, 8);
+        const uint64_t* u = in + d.a;
+        const uint64_t* v = in + d.b;
+        uint64_t* q = out + d.r;
+        uint64_t* r = out + d.r2;
+        div_cta(
+            g, smem, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
+            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; },
+            [&](uint8_t code) { if (flags) flags[d.flag] = code; });
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side: the plan
+// ---------------------------------------------------------------------------
+template <typename T>
+static bi_status dev_upload(T** dst, const std::vector<T>& v, cudaStream_t s) {
+    *dst = nullptr;
+    if (v.empty()) return BI_OK;
+    cudaError_t e = cudaMallocAsync((void**)dst, v.size() * sizeof(T), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(e == cudaErrorMemoryAllocation ? BI_ENOMEM : BI_ECUDA, "plan upload: %s",
+                         cudaGetErrorString(e));
+    }
+    return BI_OK;
+}
+
+}  // namespace bi
+
+using namespace bi;
+
+struct bi_plan {
+    int device = 0;
+    uint64_t count = 0;
+    bi_desc* d_descs = nullptr;
+    uint32_t* d_addsub = nullptr;
+    uint32_t* d_mul = nullptr;
+    uint32_t* d_div = nullptr;
+    MulItem* d_items = nullptr;
+    uint32_t* d_counters = nullptr;
+    uint32_t n_addsub = 0, n_mul = 0, n_items = 0, n_div = 0;
+    uint32_t max_mul_Lp_full = 0, max_mul_Lp_trunc = 0, max_div_mu = 0, max_div_mv = 0;
+    size_t mul_smem = 0, div_smem = 0;
+    BatchTune tune = {4, 2, 1};
+    cudaGraphExec_t exec = nullptr;
+    const void* g_in = nullptr;
+    void* g_out = nullptr;
+    void* g_flags = nullptr;
+    BatchTune g_tune = {0, 0, 0};
+    cudaStream_t cap = nullptr;
+    cudaStream_t side[3] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[3] = {};
+    std::mutex mu;
+};
+
+namespace bi {
+
+static size_t mul_smem_for(const bi_plan* p, int ipc_div) {
+    size_t best = 0;
+    for (int full = 0; full < 2; full++) {
+        const uint32_t Lp = full ? p->max_mul_Lp_full : p->max_mul_Lp_trunc;
+        if (!Lp) continue;
+        // every padded size up to the largest can appear; smaller sizes pack more instances
+        for (uint32_t L = 2 * MUL_C; L <= Lp; L += 2 * MUL_C) {
+            MulGeom g = mul_geometry(L, full != 0, 256);
+            if (ipc_div > 1 && g.ipc > 1) g = mul_geometry(L, full != 0, (g.ipc + ipc_div - 1) / ipc_div);
+            best = std::max(best, mul_smem_bytes(g));
+        }
+    }
+    return best;
+}
+
+enum { COMP_ADDSUB = 1, COMP_MUL = 2, COMP_DIV = 4, COMP_ALL = 7 };
+
+struct Launch3 {
+    unsigned grid[3];
+    size_t smem[3];
+};
+
+// Grid sizes and shared memory of the three kernels for tuning t; sets the
+// kernels' shared-memory limits (done outside any stream capture).
+static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
+    const int sms = num_sms();
+    L->grid[0] = (unsigned)std::min<uint64_t>((p->n_addsub + 7) / 8, (uint64_t)sms * 8);
+    L->smem[0] = 0;
+    L->smem[1] = mul_smem_for(p, t.mul_ipc_div);
+    L->smem[2] = p->div_smem;
+    int occ = 1;
+    if (p->n_items) {
+        if (cudaFuncSetAttribute(batch_mul_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem[1]) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_mul_kernel, BATCH_CTA, L->smem[1]) != cudaSuccess)
+            return set_error(BI_ECUDA, "batch mul kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
+        L->grid[1] = (unsigned)std::min<uint64_t>(p->n_items, (uint64_t)sms * (occ < 1 ? 1 : occ));
+    }
+    if (p->n_div) {
+        occ = 1;
+        if (cudaFuncSetAttribute(batch_div_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem[2]) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_div_kernel, BATCH_CTA, L->smem[2]) != cudaSuccess)
+            return set_error(BI_ECUDA, "batch div kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
+        L->grid[2] = (unsigned)std::min<uint64_t>(p->n_div, (uint64_t)sms * (occ < 1 ? 1 : occ));
+    }
+    return BI_OK;
+}
+
+static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags,
+                                     const BatchTune& t, const Launch3& L, cudaStream_t s_add,
+                                     cudaStream_t s_mul, cudaStream_t s_div, int comps = COMP_ALL) {
+    if (p->n_addsub && (comps & COMP_ADDSUB)) {
+        const unsigned grid = L.grid[0];
+        if (t.addsub_vec == 2 && t.addsub_rows == 4)
+            batch_addsub_kernel<2, 4><<<grid, 256, 0, s_add>>>(p->d_descs, p->d_addsub, p->n_addsub, p->d_counters + 0, in, out, flags);
+        else if (t.addsub_vec == 2 && t.addsub_rows == 2)
+            batch_addsub_kernel<2, 2><<<grid, 256, 0, s_add>>>(p->d_descs, p->d_addsub, p->n_addsub, p->d_counters + 0, in, out, flags);
+        else if (t.addsub_vec == 2)
+            batch_addsub_kernel<2, 8><<<grid, 256, 0, s_add>>>(p->d_descs, p->d_addsub, p->n_addsub, p->d_counters + 0, in, out, flags);
+        else
+            batch_addsub_kernel<1, 4><<<grid, 256, 0, s_add>>>(p->d_descs, p->d_addsub, p->n_addsub, p->d_counters + 0, in, out, flags);
+        BI_RETURN_IF(check_launch("batch add/sub kernel"));
+    }
+    if (p->n_items && (comps & COMP_MUL)) {
+        batch_mul_kernel<<<L.grid[1], BATCH_CTA, L.smem[1], s_mul>>>(p->d_descs, p->d_mul, p->d_items, p->n_items,
+                                                                     p->d_counters + 1, in, out, t.mul_ipc_div);
+        BI_RETURN_IF(check_launch("batch mul kernel"));
+    }
+    if (p->n_div && (comps & COMP_DIV)) {
+        batch_div_kernel<<<L.grid[2], BATCH_CTA, L.smem[2], s_div>>>(p->d_descs, p->d_div, p->n_div,
+                                                                     p->d_counters + 2, in, out, flags);
+        BI_RETURN_IF(check_launch("batch div kernel"));
+    }
+    return BI_OK;
+}
+
+// Capture counter reset, fork, the three persistent kernels and the join
+// into one executable graph.
+static bi_status capture_plan(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    if (p->exec) {
+        cudaGraphExecDestroy(p->exec);
+        p->exec = nullptr;
+    }
+    Launch3 L;
+    BI_RETURN_IF(prepare_launch(p, p->tune, &L));
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return set_error(BI_ECUDA, "plan capture: %s", cudaGetErrorString(e));
+    cudaMemsetAsync(p->d_counters, 0, 3 * sizeof(uint32_t), p->cap);
+    cudaEventRecord(p->ev_fork, p->cap);
+    for (int k = 0; k < 3; k++) cudaStreamWaitEvent(p->side[k], p->ev_fork, 0);
+    bi_status st = launch_plan_kernels(p, in, out, flags, p->tune, L, p->side[0], p->side[1], p->side[2]);
+    for (int k = 0; k < 3; k++) {
+        cudaEventRecord(p->ev_join[k], p->side[k]);
+        cudaStreamWaitEvent(p->cap, p->ev_join[k], 0);
+    }
+    e = cudaStreamEndCapture(p->cap, &graph);
+    if (st != BI_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return st;
+    }
+    if (e != cudaSuccess) return set_error(BI_ECUDA, "plan capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&p->exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        p->exec = nullptr;
+        return set_error(BI_ECUDA, "plan instantiate: %s", cudaGetErrorString(e));
+    }
+    p->g_in = in;
+    p->g_out = out;
+    p->g_flags = flags;
+    p->g_tune = p->tune;
+    return BI_OK;
+}
+
+static void plan_free(bi_plan* p) {
+    if (!p) return;
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    cudaFree(p->d_descs);
+    cudaFree(p->d_addsub);
+    cudaFree(p->d_mul);
+    cudaFree(p->d_div);
+    cudaFree(p->d_items);
+    cudaFree(p->d_counters);
+    for (int k = 0; k < 3; k++) {
+        if (p->side[k]) cudaStreamDestroy(p->side[k]);
+        if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
+    }
+    if (p->ev_fork) cudaEventDestroy(p->ev_fork);
+    if (p->cap) cudaStreamDestroy(p->cap);
+    delete p;
+}
+
+}  // namespace bi
+
+extern "C" {
+
+bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t count) {
+    if (!out_plan) return set_error(BI_EINVAL, "out_plan is NULL");
+    *out_plan = nullptr;
+    if (count && !descs) return set_error(BI_EINVAL, "descs is NULL");
+    if (count > 0xffffffffull) return set_error(BI_EINVAL, "too many descriptors");
+    bi_plan* p = new bi_plan();
+    cudaGetDevice(&p->device);
+    p->count = count;
+    std::vector<uint32_t> addsub, div;
+    std::vector<std::pair<uint64_t, uint32_t>> mulkeys;   // (bucket key, index)
+    for (uint64_t i = 0; i < count; i++) {
+        const bi_desc& d = descs[i];
+        if (d.m == 0 || d.m > BATCH_MAX_LIMBS) {
+            plan_free(p);
+            return set_error(d.m == 0 ? BI_EINVAL : BI_EUNSUPPORTED, "descriptor %llu: m=%u", (unsigned long long)i, d.m);
+        }
+        switch (d.op) {
+        case BI_OP_ADD:
+        case BI_OP_SUB:
+            addsub.push_back((uint32_t)i);
+            break;
+        case BI_OP_MUL:
+        case BI_OP_MULFULL: {
+            const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
+            const uint32_t full = d.op == BI_OP_MULFULL;
+            if (full && Lp > 2048) { plan_free(p); return set_error(BI_EUNSUPPORTED, "descriptor %llu: mulfull m=%u", (unsigned long long)i, d.m); }
+            if (full) p->max_mul_Lp_full = std::max(p->max_mul_Lp_full, Lp);
+            else p->max_mul_Lp_trunc = std::max(p->max_mul_Lp_trunc, Lp);
+            mulkeys.push_back({((uint64_t)full << 40) | ((uint64_t)Lp << 8), (uint32_t)i});
+            break;
+        }
+        case BI_OP_DIV:
+            if (d.mb == 0 || d.mb > d.m) {
+                plan_free(p);
+                return set_error(BI_EINVAL, "descriptor %llu: need 1 <= mb <= m", (unsigned long long)i);
+            }
+            p->max_div_mu = std::max(p->max_div_mu, d.m);
+            p->max_div_mv = std::max(p->max_div_mv, d.mb);
+            div.push_back((uint32_t)i);
+            break;
+        default:
+            plan_free(p);
+            return set_error(BI_EINVAL, "descriptor %llu: unknown op %u", (unsigned long long)i, d.op);
+        }
+    }
+    // largest first: long instances start early, short ones fill the tail
+    std::stable_sort(addsub.begin(), addsub.end(), [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
+    std::stable_sort(div.begin(), div.end(), [&](uint32_t x, uint32_t y) {
+        return (uint64_t)descs[x].m * descs[x].mb > (uint64_t)descs[y].m * descs[y].mb;
+    });
+    std::stable_sort(mulkeys.begin(), mulkeys.end(), [](const std::pair<uint64_t, uint32_t>& x,
+                                                        const std::pair<uint64_t, uint32_t>& y) {
+        return x.first > y.first;
+    });
+    std::vector<uint32_t> mul;
+    std::vector<MulItem> items;
+    for (size_t k = 0; k < mulkeys.size();) {
+        const uint64_t key = mulkeys[k].first;
+        const uint32_t full = (uint32_t)(key >> 40), Lp = (uint32_t)((key >> 8) & 0xffffffffu);
+        const MulGeom g = mul_geometry(Lp, full != 0, 256);
+        size_t end = k;
+        while (end < mulkeys.size() && mulkeys[end].first == key) end++;
+        for (size_t s = k; s < end; s += g.ipc) {
+            MulItem it;
+            it.first = (uint32_t)mul.size();
+            it.count = (uint32_t)std::min<size_t>(g.ipc, end - s);
+            it.Lp = Lp;
+            it.full = full;
+            for (size_t j = s; j < s + it.count; j++) mul.push_back(mulkeys[j].second);
+            items.push_back(it);
+        }
+        k = end;
+    }
+    p->n_addsub = (uint32_t)addsub.size();
+    p->n_mul = (uint32_t)mul.size();
+    p->n_items = (uint32_t)items.size();
+    p->n_div = (uint32_t)div.size();
+    if (p->n_div) p->div_smem = div_smem_bytes(div_geom(p->max_div_mu, p->max_div_mv, 8));
+    if (p->div_smem > 227 * 1024 || mul_smem_for(p, 1) > 227 * 1024) {
+        plan_free(p);
+        return set_error(BI_EUNSUPPORTED, "batch sizes need too much shared memory");
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
+    for (int k = 0; k < 3 && e == cudaSuccess; k++) e = cudaStreamCreateWithFlags(&p->side[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
+    for (int k = 0; k < 3 && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&p->ev_join[k], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        plan_free(p);
+        return set_error(BI_ECUDA, "plan streams: %s", cudaGetErrorString(e));
+    }
+    std::vector<bi_desc> hd(descs, descs + count);
+    bi_status st = dev_upload(&p->d_descs, hd, p->cap);
+    if (st == BI_OK) st = dev_upload(&p->d_addsub, addsub, p->cap);
+    if (st == BI_OK) st = dev_upload(&p->d_mul, mul, p->cap);
+    if (st == BI_OK) st = dev_upload(&p->d_div, div, p->cap);
+    if (st == BI_OK) st = dev_upload(&p->d_items, items, p->cap);
+    if (st == BI_OK) {
+        std::vector<uint32_t> zeros(4, 0);
+        st = dev_upload(&p->d_counters, zeros, p->cap);
+    }
+    if (st == BI_OK && cudaStreamSynchronize(p->cap) != cudaSuccess) st = set_error(BI_ECUDA, "plan upload failed");
+    if (st != BI_OK) {
+        plan_free(p);
+        return st;
+    }
+    *out_plan = p;
+    return BI_OK;
+}
+
+bi_status bi_plan_set_tuning(bi_plan* p, int addsub_rows, int addsub_vec, int mul_ipc_div) {
+    if (!p) return set_error(BI_EINVAL, "NULL plan");
+    if (!(addsub_rows == 2 || addsub_rows == 4 || addsub_rows == 8) || !(addsub_vec == 1 || addsub_vec == 2) ||
+        mul_ipc_div < 1 || mul_ipc_div > 8)
+        return set_error(BI_EINVAL, "tuning out of range");
+    if (addsub_vec == 1) addsub_rows = 4;
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->tune = {addsub_rows, addsub_vec, mul_ipc_div};
+    return BI_OK;
+}
+
+bi_status bi_plan_execute(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags, bi_stream stream) {
+    if (!p) return set_error(BI_EINVAL, "NULL plan");
+    if (p->count == 0) return BI_OK;
+    if (!in || !out) return set_error(BI_EINVAL, "NULL arena");
+    if ((uintptr_t)in % 16 || (uintptr_t)out % 16) return set_error(BI_EINVAL, "arenas must be 16-byte aligned");
+    std::lock_guard<std::mutex> lk(p->mu);
+    if (!p->exec || p->g_in != in || p->g_out != out || p->g_flags != flags ||
+        memcmp(&p->g_tune, &p->tune, sizeof(BatchTune)) != 0) {
+        BI_RETURN_IF(capture_plan(p, in, out, flags));
+    }
+    cudaError_t e = cudaGraphLaunch(p->exec, (cudaStream_t)stream);
+    if (e != cudaSuccess) return set_error(BI_ECUDA, "plan launch: %s", cudaGetErrorString(e));
+    return BI_OK;
+}
+
+// Time one component of the plan with tuning t (ms per run, median of reps).
+static float time_component(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags, const BatchTune& t,
+                            int comp, int reps) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    std::vector<float> ts;
+    Launch3 L;
+    if (prepare_launch(p, t, &L) != BI_OK) return 1e30f;
+    for (int r = 0; r < reps + 1; r++) {
+        cudaMemsetAsync(p->d_counters, 0, 3 * sizeof(uint32_t), p->cap);
+        cudaEventRecord(e0, p->cap);
+        bi_status st = launch_plan_kernels(p, in, out, flags, t, L, p->cap, p->cap, p->cap, comp);
+        cudaEventRecord(e1, p->cap);
+        cudaEventSynchronize(e1);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (st != BI_OK) ms = 1e30f;
+        if (r > 0) ts.push_back(ms);   // the first run warms up
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::sort(ts.begin(), ts.end());
+    return ts[ts.size() / 2];
+}
+
+// Pick, on this plan's own data, the add/sub rows per step (limbs per lane)
+// and limb width per lane, and the multiply instances per CTA; results land
+// in `out` exactly as an execute would write them.
+bi_status bi_plan_autotune(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags, int reps,
+                           int* chosen) {
+    if (!p) return set_error(BI_EINVAL, "NULL plan");
+    if (p->count == 0) return BI_OK;
+    if (!in || !out) return set_error(BI_EINVAL, "NULL arena");
+    if (reps < 1) reps = 1;
+    std::lock_guard<std::mutex> lk(p->mu);
+    BatchTune best = p->tune;
+    if (p->n_addsub) {
+        const int cand[4][2] = {{2, 2}, {4, 2}, {8, 2}, {4, 1}};
+        float bt = 1e30f;
+        for (auto& c : cand) {
+            BatchTune t = best;
+            t.addsub_rows = c[0];
+            t.addsub_vec = c[1];
+            const float ms = time_component(p, in, out, flags, t, COMP_ADDSUB, reps);
+            if (ms < bt) { bt = ms; best.addsub_rows = c[0]; best.addsub_vec = c[1]; }
+        }
+    }
+    if (p->n_items) {
+        float bt = 1e30f;
+        for (int d = 1; d <= 4; d *= 2) {
+            BatchTune t = best;
+            t.mul_ipc_div = d;
+            if (mul_smem_for(p, d) > 227 * 1024) continue;
+            const float ms = time_component(p, in, out, flags, t, COMP_MUL, reps);
+            if (ms < bt) { bt = ms; best.mul_ipc_div = d; }
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(p->cap);
+    if (e != cudaSuccess) return set_error(BI_ECUDA, "autotune: %s", cudaGetErrorString(e));
+    p->tune = best;
+    if (chosen) {
+        chosen[0] = best.addsub_rows;
+        chosen[1] = best.addsub_vec;
+        chosen[2] = best.mul_ipc_div;
+    }
+    return BI_OK;
+}
+
+bi_status bi_plan_destroy(bi_plan* p) {
+    if (!p) return BI_OK;
+    cudaDeviceSynchronize();
+    plan_free(p);
+    return BI_OK;
+}
+
+bi_status bi_plan_stats(const bi_plan* p, uint64_t* stats) {
+    if (!p || !stats) return set_error(BI_EINVAL, "NULL argument");
+    stats[0] = p->n_addsub;
+    stats[1] = p->n_mul;
+    stats[2] = p->n_items;
+    stats[3] = p->n_div;
+    stats[4] = p->mul_smem ? p->mul_smem : mul_smem_for(p, p->tune.mul_ipc_div);
+    stats[5] = p->div_smem;
+    return BI_OK;
+}
+
+}  // extern "C"

@@ -34,7 +34,7 @@ struct FastDiv {
     uint32_t shift;
 
     __host__ __device__ FastDiv() : d(1), magic(0), shift(0) {}
-    __host__ explicit FastDiv(uint32_t divisor) : d(divisor) {
+    __host__ __device__ explicit FastDiv(uint32_t divisor) : d(divisor) {
         uint32_t l = 0;
         while (l < 32 && (1ull << l) < divisor) l++;
         shift = l;
@@ -107,33 +107,17 @@ __device__ __forceinline__ uint32_t block_carry_in(uint32_t g, uint32_t p, bool 
     return (warp_carry_resolve(A, B, cin).carries >> lane) & 1u;
 }
 
-__device__ __forceinline__ uint32_t lane_id() {
-    uint32_t l;
-    asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
-    return l;
-}
-
-// ---------------------------------------------------------------------------
-// Streaming 16-byte global loads and stores (each limb is touched once).
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint4 ld_stream16(const void* p) {
-    uint4 v;
-    asm volatile("ld.global.nc.L1::no_allocate.L2::evict_first.v4.u32 {%0,%1,%2,%3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p));
-    return v;
-}
-
-__device__ __forceinline__ void st_stream16(void* p, uint4 v) {
-    asm volatile("st.global.cs.v4.u32 [%0], {%1,%2,%3,%4};"
-                 :: "l"(p), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w) : "memory");
-}
-
 }  // namespace bi
 
 // ---------------------------------------------------------------------------
 // Host-side status plumbing (defined in capi.cu).
 // ---------------------------------------------------------------------------
+#define BI_RETURN_IF(x)                \
+    do {                               \
+        bi_status _s = (x);            \
+        if (_s != BI_OK) return _s;    \
+    } while (0)
+
 namespace bi {
 bi_status set_error(bi_status st, const char* fmt, ...);
 bi_status check_launch(const char* what);

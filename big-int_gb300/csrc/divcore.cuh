@@ -1,0 +1,215 @@
+// divcore.cuh -- the CTA-level shifted-inverse division shared by the uniform
+// batch kernel (div.cu) and the uneven-batch kernel (batch.cu).  See div.cu
+// for the algorithm and its correspondence with the reference.
+#pragma once
+
+#include "blockops.cuh"
+
+namespace bi {
+
+constexpr int DIV_MAX_CORRECTIONS = 8;
+
+struct DivGeom {
+    uint32_t mu, mv;        // limbs per dividend / divisor in the caller's type
+    uint32_t MU, MV;        // the same in 64-bit limbs
+    uint32_t Pmax;          // largest reciprocal precision (limbs)
+    uint32_t oUn, oVn, oY, oX;
+    uint32_t oVs, oT, oProd, oW;             // phase N (Newton) offsets inside X
+    uint32_t oBig, oQ, oQV, oR, oW2;         // phases Q/R offsets inside X
+    uint32_t smem_limbs;
+};
+
+// floor((2^128 - 1) / d) - 2^64 for d >= 2^63: the low limb of a one-limb
+// reciprocal (the quotient is in (2^64, 2^65)).  Restoring long division of
+// (~d) * 2^64 + (2^64 - 1) by d; ~d < d so the quotient fits 64 bits.
+__device__ __forceinline__ uint64_t recip_limb(uint64_t d) {
+    uint64_t rem = ~d, q = 0;
+    for (int i = 0; i < 64; i++) {
+        const uint64_t top = rem >> 63;
+        rem = (rem << 1) | 1ull;
+        q <<= 1;
+        if (top || rem >= d) {
+            rem -= d;
+            q |= 1ull;
+        }
+    }
+    return q;
+}
+
+// One division on the CTA: u has g.MU 64-bit limbs, v has g.MV; load_u(i)
+// and load_v(i) supply limbs, store_q(i, x) for i < g.MU and store_r(i, x)
+// for i < g.MV receive the results, set_status(code) the status (thread 0).
+// Every thread of the CTA calls it with the same arguments.
+template <typename LoadU, typename LoadV, typename StoreQ, typename StoreR, typename SetStatus>
+__device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU load_u, LoadV load_v,
+                                        StoreQ store_q, StoreR store_r, SetStatus set_status) {
+    uint64_t* Un = smem + g.oUn;
+    uint64_t* Vn = smem + g.oVn;
+    uint64_t* Yb = smem + g.oY;
+    uint64_t* X = smem + g.oX;
+    uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + g.smem_limbs);
+    const uint32_t MU = g.MU, MV = g.MV, Pmax = g.Pmax;
+    // ---- raw operands: u into X[0, MU), v into X[MU, MU+MV)
+    uint64_t* Uraw = X;
+    uint64_t* Vraw = X + MU;
+    for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) Uraw[i] = load_u(i);
+    for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) Vraw[i] = load_v(i);
+    __syncthreads();
+    const int K = block_prec(Vraw, (int)MV, scratch);
+    if (K == 0) {                                  // division by zero
+        for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) store_q(i, 0);
+        for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) store_r(i, 0);
+        if (threadIdx.x == 0) set_status(1);
+        __syncthreads();
+        return;
+    }
+    const int s = __clzll((long long)Vraw[K - 1]);
+    block_shl_bits(Vn, Vraw, K, K, s);
+    block_shl_bits(Un, Uraw, (int)MU, (int)MU + 1, s);
+    __syncthreads();
+    const int H = block_prec(Un, (int)MU + 1, scratch);
+    if (H < K) {                                   // u < v: q = 0, r = u
+        for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) store_q(i, 0);
+        for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) store_r(i, Uraw[i]);
+        if (threadIdx.x == 0) set_status(0);
+        __syncthreads();
+        return;
+    }
+    const int Qlen = H - K + 1;
+    const int P = Qlen + 1;
+
+    // ---- shifted inverse: Y_p at Yb + (Pmax - p), p + 1 limbs
+    if (threadIdx.x == 0) {
+        Yb[Pmax - 1] = recip_limb(Vn[K - 1]);
+        Yb[Pmax] = 1;
+        Yb[Pmax + 1] = 0;
+    }
+    int sched[40];
+    int ns = 0;
+    {
+        int x = P;
+        sched[ns++] = x;
+        while (x > 2 && ns < 40) {
+            x = (x + 2) / 2;
+            sched[ns++] = x;
+        }
+    }
+    __syncthreads();
+    int p = 1;
+    uint64_t* Vs = X + g.oVs;
+    uint64_t* Tb = X + g.oT;
+    uint64_t* Pr = X + g.oProd;
+    uint64_t* Wb = X + g.oW;
+    for (int si = ns - 1; si >= 0; si--) {
+        const int pn = sched[si];
+        if (pn <= p) continue;
+        const int sl = pn + 1;
+        // divisor prefix: the top sl limbs of v (zero-extended below when K < sl)
+        for (int i = threadIdx.x; i < sl; i += blockDim.x) {
+            const int src = K - sl + i;
+            Vs[i] = src >= 0 ? Vn[src] : 0;
+        }
+        __syncthreads();
+        const uint64_t* Yp = Yb + (Pmax - p);
+        // T = Vs * Y_p mod B^(sl+1); E = B^(sl+p) - Vs*Y_p, |E| < B^(sl+1)/2
+        block_mul(Vs, sl, Yp, p + 1, Tb, sl + 1, Wb, scratch);
+        const bool e_neg = (Tb[sl] >> 63) == 0;    // T small: E = -T
+        if (!e_neg) block_addsub(Tb, nullptr, 0, Tb, sl + 1, sl + 1, true, scratch);   // |E| = -T
+        // D = floor(Y_p * |E| / B^(2p+1))
+        block_mul(Yp, p + 1, Tb, sl + 1, Pr, p + sl + 2, Wb, scratch);
+        const uint64_t* D = Pr + 2 * p + 1;
+        const int Dlen = sl - p + 1;
+        // Y_pn = Y_p * B^(pn-p) +/- D
+        for (int i = threadIdx.x; i < pn - p; i += blockDim.x) Yb[Pmax - pn + i] = 0;
+        __syncthreads();
+        uint64_t* Ypn = Yb + (Pmax - pn);
+        block_addsub(Ypn, Ypn, pn + 1, D, Dlen, pn + 1, e_neg, scratch);
+        p = pn;
+    }
+    const uint64_t* Y = Yb + (Pmax - P);
+
+    // ---- quotient estimate: floor(Un * Y / B^(P+K))
+    uint64_t* Big = X + g.oBig;
+    uint64_t* Qb = X + g.oQ;
+    uint64_t* QV = X + g.oQV;
+    uint64_t* Rb = X + g.oR;
+    uint64_t* W2 = X + g.oW2;
+    block_mul(Un, H, Y, P + 1, Big, H + P + 1, W2, scratch);
+    for (int i = threadIdx.x; i < Qlen + 1; i += blockDim.x) Qb[i] = i < Qlen ? Big[P + K + i] : 0;
+    __syncthreads();
+
+    // ---- remainder r = u - q*v from the low K+1 limbs, then corrections
+    block_mul(Qb, Qlen + 1, Vn, K, QV, K + 1, W2, scratch);
+    block_addsub(Rb, Un, K + 1, QV, K + 1, K + 1, true, scratch);
+    int fixes = 0;
+    bool ok = true;
+    while ((Rb[K] >> 63) != 0) {                  // r < 0
+        if (++fixes > DIV_MAX_CORRECTIONS) { ok = false; break; }
+        block_addsub(Rb, Rb, K + 1, Vn, K, K + 1, false, scratch);
+        // q -= 1
+        uint64_t* onebuf = QV;                     // QV is free now
+        if (threadIdx.x == 0) onebuf[0] = 1;
+        __syncthreads();
+        block_addsub(Qb, Qb, Qlen + 1, onebuf, 1, Qlen + 1, true, scratch);
+    }
+    fixes = 0;
+    while (ok && block_cmp(Rb, K + 1, Vn, K, K + 1, scratch) >= 0) {   // r >= v
+        if (++fixes > DIV_MAX_CORRECTIONS) { ok = false; break; }
+        block_addsub(Rb, Rb, K + 1, Vn, K, K + 1, true, scratch);
+        uint64_t* onebuf = QV;
+        if (threadIdx.x == 0) onebuf[0] = 1;
+        __syncthreads();
+        block_addsub(Qb, Qb, Qlen + 1, onebuf, 1, Qlen + 1, false, scratch);
+    }
+
+    // ---- outputs: q, and r shifted back by s bits
+    uint64_t* Rout = QV;
+    block_shr_bits(Rout, Rb, K, K, s);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) store_q(i, (int)i < Qlen + 1 ? Qb[i] : 0);
+    for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) store_r(i, (int)i < K ? Rout[i] : 0);
+    if (threadIdx.x == 0) set_status(ok ? 0 : 2);
+    __syncthreads();
+}
+
+__host__ __device__ inline DivGeom div_geom(uint32_t mu, uint32_t mv, int wbytes) {
+    DivGeom g;
+    g.mu = mu;
+    g.mv = mv;
+    g.MU = wbytes == 8 ? mu : (mu + 1) / 2;
+    g.MV = wbytes == 8 ? mv : (mv + 1) / 2;
+    g.Pmax = g.MU + 2;
+    const uint32_t MU = g.MU, MV = g.MV, Pm = g.Pmax;
+    g.oUn = 0;
+    g.oVn = g.oUn + MU + 2;
+    g.oY = g.oVn + MV + 2;
+    g.oX = g.oY + Pm + 4;
+    // phase N
+    g.oVs = 0;
+    g.oT = g.oVs + Pm + 4;
+    g.oProd = g.oT + Pm + 4;
+    const uint32_t prodlen = 2 * Pm + 8;
+    g.oW = g.oProd + prodlen;
+    const uint32_t endN = g.oW + (prodlen + 7) / 8 * 10 + 10;
+    // phases Q and R
+    const uint32_t biglen = MU + Pm + 4;
+    g.oBig = 0;
+    g.oQ = g.oBig + biglen;
+    g.oQV = g.oQ + Pm + 4;
+    g.oR = g.oQV + (MV + 4 > Pm + 4 ? MV + 4 : Pm + 4);
+    g.oW2 = g.oR + MV + 4;
+    const uint32_t endQ = g.oW2 + (biglen + 7) / 8 * 10 + 10;
+    // the raw operands are staged in X too
+    uint32_t endX = endN > endQ ? endN : endQ;
+    if (endX < MU + MV) endX = MU + MV;
+    g.smem_limbs = g.oX + endX;
+    return g;
+}
+
+
+__host__ __device__ inline size_t div_smem_bytes(const DivGeom& g) { return (size_t)g.smem_limbs * 8 + BLOCKOPS_SCRATCH_WORDS * 4; }
+__host__ __device__ inline int div_threads(uint32_t MU) {
+    return MU >= 1024 ? 512 : MU >= 256 ? 256 : MU >= 64 ? 128 : MU >= 16 ? 64 : 32;
+}
+
+}  // namespace bi

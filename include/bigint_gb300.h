@@ -157,6 +157,54 @@ bi_status bi_host_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
                           uint8_t* sign, uint32_t m, uint64_t n);
 
 /* ---------------------------------------------------------------------- */
+/* Uneven batches: instances of different operations and sizes in one      */
+/* graph-captured launch.  The reference launches one template-specialised */
+/* kernel per (operation, size) (cuda/main.cu:476-515); a plan instead     */
+/* buckets the descriptors once and runs persistent add/sub, multiply and  */
+/* divide kernels concurrently from one CUDA graph.  64-bit limbs only.    */
+/* ---------------------------------------------------------------------- */
+#define BI_OP_ADD      0u   /* r = (a + b) mod B^m                         */
+#define BI_OP_SUB      1u   /* r = |a - b|, flags[flag] = (a < b)          */
+#define BI_OP_MUL      2u   /* r = (a * b) mod B^m                         */
+#define BI_OP_MULFULL  3u   /* r = a * b, 2m limbs                         */
+#define BI_OP_DIV      4u   /* r = a / b (m limbs), r2 = a mod b (mb       */
+                            /* limbs), flags[flag] = status as bi_div_u64  */
+
+typedef struct bi_desc {
+    uint32_t op;        /* BI_OP_* */
+    uint32_t m;         /* limbs of a (the dividend for BI_OP_DIV) */
+    uint32_t mb;        /* limbs of b for BI_OP_DIV (1 <= mb <= m); else ignored (= m) */
+    uint32_t reserved;  /* 0 */
+    uint64_t a, b;      /* limb offsets of the operands in the input arena */
+    uint64_t r, r2;     /* limb offsets of the results in the output arena */
+    uint64_t flag;      /* byte offset of the sign / status in the flag arena */
+} bi_desc;
+
+typedef struct bi_plan bi_plan;
+
+/* Build a plan from host descriptors (m <= 2048; mulfull m <= 2048).      */
+/* Allocates device work lists; the plan is bound to the current device.   */
+bi_status bi_plan_create(bi_plan** plan, const bi_desc* descs, uint64_t count);
+/* Run the plan: in/out are device arenas (16-byte aligned), flags may be   */
+/* NULL.  The first call (and any call with other arenas or tuning)        */
+/* captures the CUDA graph; later calls replay it on `stream`.  Calls on    */
+/* one plan are serialised; its launches must not overlap on the device.   */
+bi_status bi_plan_execute(bi_plan* plan, const uint64_t* in, uint64_t* out,
+                          uint8_t* flags, bi_stream stream);
+/* Time candidate configurations on this plan's data and keep the fastest: */
+/* add/sub rows per step (2/4/8 x 16 bytes per lane) and limb width per    */
+/* lane (8 or 16 bytes), multiply instances per CTA (default / 2 / 4).     */
+/* chosen (may be NULL) receives {rows, limbs per lane, ipc divisor}.      */
+bi_status bi_plan_autotune(bi_plan* plan, const uint64_t* in, uint64_t* out,
+                           uint8_t* flags, int reps, int* chosen);
+bi_status bi_plan_set_tuning(bi_plan* plan, int addsub_rows, int addsub_vec,
+                             int mul_ipc_div);
+/* stats[0..5] = add/sub instances, multiply instances, multiply items,    */
+/* divisions, multiply and divide shared-memory bytes per CTA.             */
+bi_status bi_plan_stats(const bi_plan* plan, uint64_t* stats);
+bi_status bi_plan_destroy(bi_plan* plan);
+
+/* ---------------------------------------------------------------------- */
 /* Synthetic inputs: dst[i] = splitmix64 output number offset+i+1 of the   */
 /* stream `seed`.  No counterpart in the reference, whose benchmarks draw  */
 /* unseeded rand() digits (cuda/helpers.h:96-111); this makes multi-GiB    */

@@ -1,0 +1,166 @@
+"""GPU parity of the uneven-batch plan (bi_plan_*): every instance of a mixed
+batch of add, sub, full multiply and division over sizes log-uniform in
+256..8192 bits is compared with the oracle; large instances of each
+operation; graph replay, recapture on new arenas and autotuning leave the
+results unchanged; invalid descriptors are rejected."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _groups(d):
+    keys = {}
+    for i, (op, m, mb) in enumerate(zip(d["op"], d["m"], d["mb"])):
+        keys.setdefault((int(op), int(m), int(mb)), []).append(i)
+    return keys
+
+
+def check_batch(B, oracle, d, arena, out, flags):
+    """Compare every instance of the batch with the oracle, grouped by shape."""
+    for (op, m, mb), idx in _groups(d).items():
+        idx = np.array(idx)
+        a = np.stack([arena[d["a"][i]: d["a"][i] + m] for i in idx])
+        b = np.stack([arena[d["b"][i]: d["b"][i] + mb] for i in idx])
+        if op == B.OP_ADD:
+            got = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
+            assert (got == oracle.add(a, b)).all(), ("add", m)
+        elif op == B.OP_SUB:
+            got = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
+            r, s = oracle.sub(a, b)
+            assert (got == r).all(), ("sub", m)
+            assert (flags[d["flag"][idx]] == s).all(), ("sub sign", m)
+        elif op == B.OP_MULFULL:
+            got = np.stack([out[d["r"][i]: d["r"][i] + 2 * m] for i in idx])
+            assert (got == oracle.mulfull(a, b)).all(), ("mulfull", m)
+        elif op == B.OP_MUL:
+            got = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
+            assert (got == oracle.mul(a, b)).all(), ("mul", m)
+        else:
+            q = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
+            r = np.stack([out[d["r2"][i]: d["r2"][i] + mb] for i in idx])
+            qo, ro, so = oracle.div(a, b)
+            assert (q == qo).all() and (r == ro).all(), ("div", m, mb)
+            assert (flags[d["flag"][idx]] == so).all()
+
+
+def _run(B, d, arena, out_limbs, nflags, tune=None, autotune=False):
+    import torch
+
+    din = B.to_device(arena)
+    dout = torch.zeros(max(1, out_limbs), dtype=torch.int64, device="cuda")
+    dfl = torch.zeros(max(1, nflags), dtype=torch.uint8, device="cuda")
+    plan = B.Plan(d)
+    if tune:
+        plan.set_tuning(*tune)
+    if autotune:
+        plan.autotune(din, dout, dfl, reps=1)
+    plan.execute(din, dout, dfl)
+    torch.cuda.synchronize()
+    return plan, din, dout, dfl
+
+
+def test_uneven_batch_small_sizes(bigint, oracle):
+    B = bigint
+    d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=3000, seed=77, max_bits=8192)
+    plan, din, dout, dfl = _run(B, d, arena, out_limbs, nflags)
+    check_batch(B, oracle, d, arena, B.to_host(dout, np.uint64), dfl.cpu().numpy())
+    st = plan.stats()
+    assert st["addsub"] + st["mul"] + st["div"] == len(d)
+    plan.close()
+
+
+@pytest.mark.parametrize("tune", [(2, 2, 1), (8, 2, 2), (4, 1, 4)])
+def test_tunings_agree(bigint, oracle, tune):
+    B = bigint
+    d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=800, seed=78, max_bits=16384)
+    plan, din, dout, dfl = _run(B, d, arena, out_limbs, nflags, tune=tune)
+    check_batch(B, oracle, d, arena, B.to_host(dout, np.uint64), dfl.cpu().numpy())
+    plan.close()
+
+
+def test_autotune_then_replay_and_recapture(bigint, oracle):
+    import torch
+
+    B = bigint
+    d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=1500, seed=79, max_bits=4096)
+    plan, din, dout, dfl = _run(B, d, arena, out_limbs, nflags, autotune=True)
+    first = dout.clone()
+    dout.zero_()
+    plan.execute(din, dout, dfl)                  # graph replay
+    torch.cuda.synchronize()
+    assert bool((dout == first).all())
+    dout2 = torch.zeros_like(dout)
+    plan.execute(din, dout2, dfl)                 # new arena: recapture
+    torch.cuda.synchronize()
+    assert bool((dout2 == first).all())
+    check_batch(B, oracle, d, arena, B.to_host(dout2, np.uint64), dfl.cpu().numpy())
+    plan.close()
+
+
+def test_large_instances(bigint, oracle):
+    """The largest sizes the batch accepts, one op at a time, with unaligned offsets."""
+    B = bigint
+    rows = []
+    arena = []
+    off = 1                                       # odd limb offsets: the 8-byte path
+    out = 0
+    for op, m, mb in [(B.OP_ADD, 2048, 2048), (B.OP_SUB, 1500, 1500), (B.OP_MULFULL, 1024, 1024),
+                      (B.OP_MUL, 2048, 2048), (B.OP_DIV, 2048, 1024), (B.OP_DIV, 1000, 3)]:
+        a = B.workloads.uniform_limbs(500 + m + op, 1, m)[0]
+        b = B.workloads.uniform_limbs(600 + m + op, 1, mb)[0]
+        b[-1] |= np.uint64(1)
+        rows.append((op, m, mb, off, off + m, out))
+        arena += [a, b]
+        off += m + mb
+        out += 3 * m + mb
+    d = np.zeros(len(rows), dtype=B.DESC_DTYPE)
+    for i, (op, m, mb, ao, bo, ro) in enumerate(rows):
+        d[i] = (op, m, mb, 0, ao, bo, ro, ro + (2 * m if op != B.OP_DIV else m), i)
+    ar = np.concatenate([np.zeros(1, np.uint64)] + arena)
+    plan, din, dout, dfl = _run(B, d, ar, out, len(d))
+    check_batch(B, oracle, d, ar, B.to_host(dout, np.uint64), dfl.cpu().numpy())
+    plan.close()
+
+
+def test_batch_matches_per_size_kernels(bigint):
+    """The batch and the plain one-launch-per-size kernels give the same results."""
+    import torch
+
+    B = bigint
+    d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=2000, seed=80, max_bits=32768)
+    plan, din, dout, dfl = _run(B, d, arena, out_limbs, nflags)
+    out = B.to_host(dout, np.uint64)
+    for (op, m, mb), idx in _groups(d).items():
+        idx = np.array(idx)
+        a = B.to_device(np.stack([arena[d["a"][i]: d["a"][i] + m] for i in idx]))
+        b = B.to_device(np.stack([arena[d["b"][i]: d["b"][i] + mb] for i in idx]))
+        if op == B.OP_ADD:
+            ref = B.to_host(B.add(a, b), np.uint64)
+            got = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
+        elif op == B.OP_SUB:
+            ref = B.to_host(B.sub(a, b)[0], np.uint64)
+            got = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
+        elif op == B.OP_MULFULL:
+            ref = B.to_host(B.mulfull(a, b), np.uint64)
+            got = np.stack([out[d["r"][i]: d["r"][i] + 2 * m] for i in idx])
+        else:
+            q, r, _ = B.div(a, b)
+            ref = np.concatenate([B.to_host(q, np.uint64), B.to_host(r, np.uint64)], axis=1)
+            got = np.stack([np.concatenate([out[d["r"][i]: d["r"][i] + m], out[d["r2"][i]: d["r2"][i] + mb]])
+                            for i in idx])
+        assert (got == ref).all(), (op, m)
+    plan.close()
+    torch.cuda.synchronize()
+
+
+def test_invalid_descriptors_rejected(bigint):
+    B = bigint
+    d = np.zeros(1, dtype=B.DESC_DTYPE)
+    for bad in [dict(op=0, m=0, mb=0), dict(op=9, m=4, mb=4), dict(op=4, m=4, mb=5), dict(op=0, m=5000, mb=5000)]:
+        d[0]["op"], d[0]["m"], d[0]["mb"] = bad["op"], bad["m"], bad["mb"]
+        with pytest.raises(B.BigIntError):
+            B.Plan(d)
+    empty = B.Plan(np.zeros(0, dtype=B.DESC_DTYPE))
+    assert empty.stats()["addsub"] == 0
+    empty.close()
