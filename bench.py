@@ -287,9 +287,71 @@ def measure_extra(B, L, stream, args):
         div[f"m{mv}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4)}
         del u, v, q, rr, st
     out["div_u64_2m_by_m"] = div
+    out["uneven_batch"] = measure_uneven_batch(B, L, stream)
     out["reference_cuda_kernels"] = measure_reference_kernels(B, L, stream)
     torch.cuda.empty_cache()
     return out
+
+
+def measure_uneven_batch(B, L, stream, n: int = 100_000):
+    """100k mixed instances (sizes log-uniform 256..65536 bits; 20% add, 20% sub,
+    40% full multiply, 20% division): one graph-captured plan launch versus the
+    plain one-launch-per-(op, size) kernels on the same instances."""
+    import torch
+
+    d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=n)
+    din = B.to_device(arena)
+    dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
+    dfl = torch.zeros(nflags, dtype=torch.uint8, device="cuda")
+    t0 = time.perf_counter()
+    plan = B.Plan(d)
+    plan_ms = (time.perf_counter() - t0) * 1e3
+    chosen = plan.autotune(din, dout, dfl, reps=2)
+    ms_batch = event_time(stream, lambda: plan.execute(din, dout, dfl, stream=stream), 5, 2)
+    # plain per-size launches: operands regrouped per (op, m) (untimed), one launch per group
+    sp = int(stream.cuda_stream)
+    groups = {}
+    for i, key in enumerate(zip(d["op"].tolist(), d["m"].tolist(), d["mb"].tolist())):
+        groups.setdefault(key, []).append(i)
+    calls = []
+    for (op, m, mb), idx in groups.items():
+        idx = np.asarray(idx)
+        ia = torch.from_numpy((d["a"][idx][:, None] + np.arange(m)[None, :]).astype(np.int64)).cuda()
+        ib = torch.from_numpy((d["b"][idx][:, None] + np.arange(mb)[None, :]).astype(np.int64)).cuda()
+        a, b = din[ia].contiguous(), din[ib].contiguous()
+        g = len(idx)
+        if op in (B.OP_ADD, B.OP_SUB):
+            r = torch.empty_like(a)
+            s = torch.empty(g, dtype=torch.uint8, device="cuda")
+            calls.append((op, a, b, r, s, m, mb, g))
+        elif op == B.OP_MULFULL:
+            calls.append((op, a, b, torch.empty((g, 2 * m), dtype=torch.int64, device="cuda"), None, m, mb, g))
+        else:
+            calls.append((op, a, b, (torch.empty_like(a), torch.empty_like(b)),
+                          torch.empty(g, dtype=torch.uint8, device="cuda"), m, mb, g))
+
+    def per_size():
+        for op, a, b, r, s, m, mb, g in calls:
+            if op == B.OP_ADD:
+                check(L, L.bi_add_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, g, sp))
+            elif op == B.OP_SUB:
+                check(L, L.bi_sub_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), s.data_ptr(), m, g, sp))
+            elif op == B.OP_MULFULL:
+                check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, g, sp))
+            else:
+                check(L, L.bi_div_u64(a.data_ptr(), b.data_ptr(), r[0].data_ptr(), r[1].data_ptr(), s.data_ptr(),
+                                      m, mb, g, sp))
+
+    ms_per_size = event_time(stream, per_size, 2, 1)
+    st = plan.stats()
+    plan.close()
+    del din, dout, dfl, calls
+    torch.cuda.empty_cache()
+    return {"instances": n, "batched_inst_per_s": round(n / ms_batch * 1e3), "batched_ms": round(ms_batch, 3),
+            "per_size_launch_inst_per_s": round(n / ms_per_size * 1e3), "per_size_launch_ms": round(ms_per_size, 3),
+            "speedup_vs_per_size_launch": round(ms_per_size / ms_batch, 2), "per_size_launches": len(groups),
+            "plan_create_ms": round(plan_ms, 1), "autotune": chosen, "plan": st,
+            "note": "one CUDA-graph replay of three concurrent persistent kernels vs one plain launch per (op, m) group"}
 
 
 def measure_reference_kernels(B, L, stream):
