@@ -107,6 +107,8 @@ SIGNATURES: dict[str, list] = {
     "bi_plan_set_tuning": [_P, _I, _I, _I],
     "bi_plan_stats": [_P, _P],
     "bi_plan_destroy": [_P],
+    "bi_batch_noalloc_max_descs": [],
+    "bi_batch_run_noalloc": [_P, _U64, _P, _P, _P, _P],
     "bi_probe_intpipe": [_P, _P],
 }
 _RESTYPE = {
@@ -118,6 +120,7 @@ _RESTYPE = {
     "bi_max_limbs_mul_u32": _U32,
     "bi_max_limbs_div_u64": _U32,
     "bi_max_limbs_div_u32": _U32,
+    "bi_batch_noalloc_max_descs": _U32,
 }
 
 

@@ -645,3 +645,161 @@ bi_status bi_plan_stats(const bi_plan* p, uint64_t* stats) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Uneven batch without any device allocation.
+//
+// bi_plan_create allocates device work lists and counters.  Some callers
+// cannot allocate device memory at the point where they need a batch run --
+// code running under an allocator that forbids cudaMalloc, or inside a
+// framework callback that must not allocate -- so this entry point keeps the
+// same scratch (a copy of the descriptors, the three work lists, the
+// multiply items and the work counters) in a fixed array in device memory
+// that the library owns, and launches the same three persistent kernels on
+// the caller's stream.  The array is a file-scope __device__ variable: every
+// GPU that loads the library holds NOALLOC_SCRATCH_BYTES of it until the
+// process exits, and all calls share it.
+// ---------------------------------------------------------------------------
+namespace bi {
+
+constexpr uint32_t NOALLOC_MAX_DESCS = 4096;
+constexpr size_t NA_DESC_OFF = 0;
+constexpr size_t NA_ADD_OFF = NA_DESC_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(bi_desc);
+constexpr size_t NA_MUL_OFF = NA_ADD_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(uint32_t);
+constexpr size_t NA_DIV_OFF = NA_MUL_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(uint32_t);
+constexpr size_t NA_ITEM_OFF = NA_DIV_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(uint32_t);
+constexpr size_t NA_CNT_OFF = NA_ITEM_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(MulItem);
+constexpr size_t NOALLOC_SCRATCH_BYTES = NA_CNT_OFF + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Host-side staging of the work lists, reused by every call (no heap use).
+static bi_desc na_descs[NOALLOC_MAX_DESCS];
+static uint32_t na_add[NOALLOC_MAX_DESCS], na_mul[NOALLOC_MAX_DESCS], na_div[NOALLOC_MAX_DESCS];
+static std::pair<uint64_t, uint32_t> na_keys[NOALLOC_MAX_DESCS];
+static MulItem na_items[NOALLOC_MAX_DESCS];
+static std::mutex na_mu;                 // guards the staging arrays and the address cache
+static void* na_dev_ptr[256];            // device address of the scratch array, per device
+
+// Device address of the scratch array on the current device, looked up on
+// the first call for that device (the host symbol is not a device address).
+static bi_status noalloc_scratch(void** ptr) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess || dev < 0 || dev >= 256) return set_error(BI_ECUDA, "no current device");
+    if (!na_dev_ptr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || p == nullptr) {
+            cudaGetLastError();
+            return set_error(BI_ECUDA, "scratch address lookup: %s", cudaGetErrorString(e));
+        }
+        na_dev_ptr[dev] = p;
+    }
+    *ptr = na_dev_ptr[dev];
+    return BI_OK;
+}
+
+}  // namespace bi
+
+extern "C" uint32_t bi_batch_noalloc_max_descs(void) { return NOALLOC_MAX_DESCS; }
+
+extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, const uint64_t* in, uint64_t* out,
+                                          uint8_t* flags, bi_stream stream) {
+    if (count == 0) return BI_OK;
+    if (!descs) return set_error(BI_EINVAL, "descs is NULL");
+    if (count > NOALLOC_MAX_DESCS)
+        return set_error(BI_EINVAL, "bi_batch_run_noalloc takes at most %u descriptors, got %llu (use bi_plan_*)",
+                         NOALLOC_MAX_DESCS, (unsigned long long)count);
+    if (!in || !out) return set_error(BI_EINVAL, "NULL arena");
+    if ((uintptr_t)in % 16 || (uintptr_t)out % 16) return set_error(BI_EINVAL, "arenas must be 16-byte aligned");
+    std::lock_guard<std::mutex> lk(na_mu);
+    void* scratch = nullptr;
+    BI_RETURN_IF(noalloc_scratch(&scratch));
+    unsigned char* base = (unsigned char*)scratch;
+
+    // the work lists, exactly as bi_plan_create builds them
+    bi_plan p;                            // on the stack; owns nothing
+    uint32_t na = 0, nm = 0, nd = 0, nk = 0, ni = 0;
+    for (uint64_t i = 0; i < count; i++) {
+        const bi_desc& d = descs[i];
+        na_descs[i] = d;
+        if (d.m == 0 || d.m > BATCH_MAX_LIMBS)
+            return set_error(d.m == 0 ? BI_EINVAL : BI_EUNSUPPORTED, "descriptor %llu: m=%u", (unsigned long long)i, d.m);
+        if (d.op == BI_OP_ADD || d.op == BI_OP_SUB) {
+            na_add[na++] = (uint32_t)i;
+        } else if (d.op == BI_OP_MUL || d.op == BI_OP_MULFULL) {
+            const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
+            const uint32_t full = d.op == BI_OP_MULFULL;
+            if (full && Lp > 2048) return set_error(BI_EUNSUPPORTED, "descriptor %llu: mulfull m=%u", (unsigned long long)i, d.m);
+            if (full) p.max_mul_Lp_full = std::max(p.max_mul_Lp_full, Lp);
+            else p.max_mul_Lp_trunc = std::max(p.max_mul_Lp_trunc, Lp);
+            na_keys[nk++] = {((uint64_t)full << 40) | ((uint64_t)Lp << 8), (uint32_t)i};
+        } else if (d.op == BI_OP_DIV) {
+            if (d.mb == 0 || d.mb > d.m) return set_error(BI_EINVAL, "descriptor %llu: need 1 <= mb <= m", (unsigned long long)i);
+            p.max_div_mu = std::max(p.max_div_mu, d.m);
+            p.max_div_mv = std::max(p.max_div_mv, d.mb);
+            na_div[nd++] = (uint32_t)i;
+        } else {
+            return set_error(BI_EINVAL, "descriptor %llu: unknown op %u", (unsigned long long)i, d.op);
+        }
+    }
+    std::stable_sort(na_add, na_add + na, [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
+    std::stable_sort(na_div, na_div + nd, [&](uint32_t x, uint32_t y) {
+        return (uint64_t)descs[x].m * descs[x].mb > (uint64_t)descs[y].m * descs[y].mb;
+    });
+    std::stable_sort(na_keys, na_keys + nk, [](const std::pair<uint64_t, uint32_t>& x,
+                                               const std::pair<uint64_t, uint32_t>& y) { return x.first > y.first; });
+    for (uint32_t k = 0; k < nk;) {
+        const uint64_t key = na_keys[k].first;
+        const uint32_t full = (uint32_t)(key >> 40), Lp = (uint32_t)((key >> 8) & 0xffffffffu);
+        const MulGeom g = mul_geometry(Lp, full != 0, 256);
+        uint32_t end = k;
+        while (end < nk && na_keys[end].first == key) end++;
+        for (uint32_t s = k; s < end; s += g.ipc) {
+            MulItem it;
+            it.first = nm;
+            it.count = std::min<uint32_t>(g.ipc, end - s);
+            it.Lp = Lp;
+            it.full = full;
+            for (uint32_t j = s; j < s + it.count; j++) na_mul[nm++] = na_keys[j].second;
+            na_items[ni++] = it;
+        }
+        k = end;
+    }
+    p.count = count;
+    p.n_addsub = na;
+    p.n_mul = nm;
+    p.n_items = ni;
+    p.n_div = nd;
+    if (nd) p.div_smem = div_smem_bytes(div_geom(p.max_div_mu, p.max_div_mv, 8));
+    if (p.div_smem > 227 * 1024 || mul_smem_for(&p, 1) > 227 * 1024)
+        return set_error(BI_EUNSUPPORTED, "batch sizes need too much shared memory");
+    p.d_descs = (bi_desc*)(base + NA_DESC_OFF);
+    p.d_addsub = (uint32_t*)(base + NA_ADD_OFF);
+    p.d_mul = (uint32_t*)(base + NA_MUL_OFF);
+    p.d_div = (uint32_t*)(base + NA_DIV_OFF);
+    p.d_items = (MulItem*)(base + NA_ITEM_OFF);
+    p.d_counters = (uint32_t*)(base + NA_CNT_OFF);
+
+    // stage the lists (the array keeps the previous call's contents: every
+    // region read below is rewritten, and the counters are cleared)
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaError_t e = cudaMemcpyAsync(p.d_descs, na_descs, count * sizeof(bi_desc), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && na) e = cudaMemcpyAsync(p.d_addsub, na_add, na * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nm) e = cudaMemcpyAsync(p.d_mul, na_mul, nm * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && nd) e = cudaMemcpyAsync(p.d_div, na_div, nd * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && ni) e = cudaMemcpyAsync(p.d_items, na_items, ni * sizeof(MulItem), cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.d_counters, 0, 3 * sizeof(uint32_t), s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(BI_ECUDA, "staging the batch: %s", cudaGetErrorString(e));
+    }
+    Launch3 L;
+    BI_RETURN_IF(prepare_launch(&p, p.tune, &L));
+    BI_RETURN_IF(launch_plan_kernels(&p, in, out, flags, p.tune, L, s, s, s));
+    // the host staging arrays may be reused once the copies have read them
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return set_error(BI_ECUDA, "batch run: %s", cudaGetErrorString(e));
+    return BI_OK;
+}

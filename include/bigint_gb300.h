@@ -205,6 +205,27 @@ bi_status bi_plan_stats(const bi_plan* plan, uint64_t* stats);
 bi_status bi_plan_destroy(bi_plan* plan);
 
 /* ---------------------------------------------------------------------- */
+/* Uneven batch that allocates nothing.  No counterpart in the reference.  */
+/* For callers that cannot allocate device memory where they need a batch  */
+/* run (an allocator that forbids cudaMalloc, a callback that must not     */
+/* allocate): the scratch that bi_plan_create allocates -- a copy of the   */
+/* descriptors, the work lists and the work counters -- lives instead in a */
+/* fixed device array owned by the library (about 344 KB, held on every    */
+/* GPU that loads the library until the process exits).  At most          */
+/* bi_batch_noalloc_max_descs() descriptors (4096) per call; larger counts */
+/* are rejected with BI_EINVAL.  Same descriptors, arenas and results as   */
+/* bi_plan_execute; descs is host memory.  The first call on each device   */
+/* looks up the array's device address, so make it before any stream      */
+/* capture.  Every call shares the one array: calls that overlap on the    */
+/* GPU race, so issue them one after another (the call returns when its    */
+/* work on `stream` has finished).                                         */
+/* ---------------------------------------------------------------------- */
+uint32_t bi_batch_noalloc_max_descs(void);
+bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count,
+                               const uint64_t* in, uint64_t* out, uint8_t* flags,
+                               bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
 /* Synthetic inputs: dst[i] = splitmix64 output number offset+i+1 of the   */
 /* stream `seed`.  No counterpart in the reference, whose benchmarks draw  */
 /* unseeded rand() digits (cuda/helpers.h:96-111); this makes multi-GiB    */
