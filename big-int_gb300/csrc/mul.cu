@@ -75,7 +75,9 @@ static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n
     constexpr int C = MUL_C;
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
-    MulGeom g = mul_geometry(L, FULL, n < 256 ? (uint32_t)n : 256u);
+    // at least two CTAs per SM when the batch is small: fewer instances per CTA
+    const uint64_t fill = (n + 2ull * num_sms() - 1) / (2ull * num_sms());
+    MulGeom g = mul_geometry(L, FULL, fill < 256 ? (uint32_t)(fill ? fill : 1) : 256u);
     g.m = m;
     g.out_words = FULL ? 2 * m : m;
     const uint32_t threads = (g.ipc * g.tpi + 31) / 32 * 32;
