@@ -28,8 +28,9 @@ Multi-GPU: instances are independent, so N ranks run N replicas of the step
 (weak scaling, no collective on the data path; NCCL only carries the barrier
 and the max over ranks of the elapsed time).
 
-`--workload add|sub|mul|mul2048|div` with `--bits`, `--total-limbs-log2`,
-`--mul-m`, `--div-m` runs one operation on one size (used for profiling).
+`--workload add|sub|mul|div|batch` with `--bits`, `--total-limbs-log2`,
+`--mul-m`, `--div-m`, `--batch-n` runs one operation on one size, or the
+uneven batch, alone (used for profiling).
 """
 from __future__ import annotations
 
@@ -458,6 +459,15 @@ def run_single(args) -> None:
         ms = event_time(stream, lambda: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
                                                                st.data_ptr(), 2 * mv, mv, n, sp)), args.steps, args.warmup)
         print(json.dumps({"workload": w, "m": mv, "n": n, "ms": ms, "instances_per_s": n / ms * 1e3}))
+    elif w == "batch":
+        d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=args.batch_n)
+        din = B.to_device(arena)
+        dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
+        dfl = torch.zeros(nflags, dtype=torch.uint8, device="cuda")
+        plan = B.Plan(d)
+        ms = event_time(stream, lambda: plan.execute(din, dout, dfl, stream=stream), args.steps, args.warmup)
+        plan.close()
+        print(json.dumps({"workload": w, "n": args.batch_n, "ms": ms, "instances_per_s": args.batch_n / ms * 1e3}))
     else:
         raise SystemExit(f"unknown workload {w}")
 
@@ -632,11 +642,12 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="addsub", choices=["addsub", "add", "sub", "mul", "div"])
+    ap.add_argument("--workload", default="addsub", choices=["addsub", "add", "sub", "mul", "div", "batch"])
     ap.add_argument("--bits", type=int, default=0, help="restrict the add/sub sweep to one size")
     ap.add_argument("--total-limbs-log2", type=int, default=27)
     ap.add_argument("--mul-m", type=int, default=1024)
     ap.add_argument("--div-m", type=int, default=256)
+    ap.add_argument("--batch-n", type=int, default=100_000)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
