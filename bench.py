@@ -290,6 +290,7 @@ def measure_extra(B, L, stream, args):
     out["div_u64_2m_by_m"] = div
     out["uneven_batch"] = measure_uneven_batch(B, L, stream)
     out["reference_cuda_kernels"] = measure_reference_kernels(B, L, stream)
+    out["serving"] = measure_serving(B)
     torch.cuda.empty_cache()
     return out
 
@@ -353,6 +354,55 @@ def measure_uneven_batch(B, L, stream, n: int = 100_000):
             "speedup_vs_per_size_launch": round(ms_per_size / ms_batch, 2), "per_size_launches": len(groups),
             "plan_create_ms": round(plan_ms, 1), "autotune": chosen, "plan": st,
             "note": "one CUDA-graph replay of three concurrent persistent kernels vs one plain launch per (op, m) group"}
+
+
+def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100_000, streams: int = 4):
+    """Poisson streams of requests (sizes log-uniform 512..32768 bits; 15% add,
+    15% sub, 40% full multiply, 30% division; operands resident in a 2^24-limb
+    device pool; a 2^26-limb result arena as the HBM budget): the
+    device-resident loop versus one library launch per request round-robin
+    over `streams` streams.  Latency runs from a request's arrival to the
+    host seeing its completion."""
+    import torch
+
+    from bigint_gb300.workloads import SERVE_RATES, serve_pool_device, serve_stream
+
+    pool_limbs = 1 << 24
+    _, _, pool_seed = serve_stream(1, 1.0, pool_limbs=pool_limbs)
+    pool = serve_pool_device(pool_limbs, pool_seed)
+    arena = torch.empty(1 << 26, dtype=torch.int64, device="cuda")
+    torch.cuda.synchronize()
+    rates = rates or SERVE_RATES
+    streams_of = {r: serve_stream(int(min(max_requests, max(2000, r * seconds))), r, pool_limbs=pool_limbs)
+                  for r in rates}
+    warm = serve_stream(2000, 100_000, seed=9, pool_limbs=pool_limbs)
+    keep = ("requests", "launches", "busy", "achieved_rps", "offered_rps", "p50_us", "p90_us", "p99_us",
+            "p999_us", "max_us", "mean_us")
+
+    def short(rep):
+        return {k: (round(rep[k], 2) if isinstance(rep[k], float) else rep[k]) for k in keep}
+
+    out = {}
+    with B.Server(pool, arena) as srv:
+        info = srv.info()
+        srv.replay(warm[0], warm[1])
+        for r in rates:
+            d, arr, _ = streams_of[r]
+            _, _, rep = srv.replay(d, arr)
+            out[str(r)] = {"loop": short(rep)}
+    # the loop has stopped: the per-request launches get the whole GPU
+    B.replay_plain(pool, arena, warm[0], warm[1], streams=streams)
+    for r in rates:
+        d, arr, _ = streams_of[r]
+        _, _, rep = B.replay_plain(pool, arena, d, arr, streams=streams)
+        out[str(r)]["per_request_launch"] = short(rep)
+        lo, pl = out[str(r)]["loop"], out[str(r)]["per_request_launch"]
+        out[str(r)]["p99_ratio_launch_over_loop"] = round(pl["p99_us"] / lo["p99_us"], 2) if lo["p99_us"] else None
+    del pool, arena
+    torch.cuda.empty_cache()
+    return {"rates_rps": out, "loop_ctas": info["ctas"], "loop_smem_bytes": info["smem_bytes"],
+            "result_arena_limbs": info["arena_limbs"], "per_request_streams": streams,
+            "note": "open-loop Poisson replay; latency = completion seen by the host - scheduled arrival"}
 
 
 def measure_reference_kernels(B, L, stream):
@@ -468,6 +518,9 @@ def run_single(args) -> None:
         ms = event_time(stream, lambda: plan.execute(din, dout, dfl, stream=stream), args.steps, args.warmup)
         plan.close()
         print(json.dumps({"workload": w, "n": args.batch_n, "ms": ms, "instances_per_s": args.batch_n / ms * 1e3}))
+    elif w == "serve":
+        rates = [args.serve_rate] if args.serve_rate else None
+        print(json.dumps({"workload": w, "serving": measure_serving(B, rates=rates)}))
     else:
         raise SystemExit(f"unknown workload {w}")
 
@@ -643,12 +696,13 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="addsub", choices=["addsub", "add", "sub", "mul", "div", "batch"])
+    ap.add_argument("--workload", default="addsub", choices=["addsub", "add", "sub", "mul", "div", "batch", "serve"])
     ap.add_argument("--bits", type=int, default=0, help="restrict the add/sub sweep to one size")
     ap.add_argument("--total-limbs-log2", type=int, default=27)
     ap.add_argument("--mul-m", type=int, default=1024)
     ap.add_argument("--div-m", type=int, default=256)
     ap.add_argument("--batch-n", type=int, default=100_000)
+    ap.add_argument("--serve-rate", type=int, default=0, help="serve workload: one offered load (requests/s)")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

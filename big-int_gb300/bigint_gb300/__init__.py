@@ -110,6 +110,14 @@ SIGNATURES: dict[str, list] = {
     "bi_batch_noalloc_max_descs": [],
     "bi_batch_run_noalloc": [_P, _U64, _P, _P, _P, _P],
     "bi_probe_intpipe": [_P, _P],
+    "bi_server_create": [_P, _P, _U64, _P, _U64, _U32, _U32, _U32, _U32],
+    "bi_server_submit": [_P, _P, _P],
+    "bi_server_poll": [_P, _P, _U32, _P],
+    "bi_server_release": [_P, _U64],
+    "bi_server_info": [_P, _P],
+    "bi_server_destroy": [_P],
+    "bi_server_replay": [_P, _P, _P, _U64, _P, _P, _P],
+    "bi_serve_replay_plain": [_P, _P, _U64, _P, _P, _U64, _U32, _P, _P, _P],
 }
 _RESTYPE = {
     "bi_status_string": ctypes.c_char_p,
@@ -307,6 +315,108 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# serving loop (include/bigint_gb300.h: bi_server_*)
+# ---------------------------------------------------------------------------
+
+BI_EBUSY = 7
+
+COMPLETION_DTYPE = np.dtype([("ticket", "<u8"), ("r", "<u8"), ("r2", "<u8"), ("status", "<u4"), ("op", "<u4")])
+REPORT_KEYS = ("requests", "launches", "busy", "duration_s", "offered_rps", "achieved_rps",
+               "p50_us", "p90_us", "p99_us", "p999_us", "max_us", "mean_us")
+
+
+def _report(buf) -> dict:
+    return dict(zip(REPORT_KEYS, [float(x) for x in buf]))
+
+
+class Server:
+    """A device-resident request loop over the operand arena `operands`
+    (a uint64 CUDA tensor).  `arena` (a uint64 CUDA tensor) receives the
+    results; its size is the server's memory budget for results in flight."""
+
+    def __init__(self, operands, arena, ring_slots: int = 0, max_limbs: int = 0, ctas: int = 0,
+                 idle_us: int = 0):
+        self.operands, self.arena = operands, arena
+        self._h = ctypes.c_void_p()
+        _check(lib().bi_server_create(ctypes.byref(self._h), operands.data_ptr(), operands.numel(),
+                                      arena.data_ptr(), arena.numel(), ring_slots, max_limbs, ctas, idle_us))
+
+    def submit(self, desc):
+        """Ticket of the admitted request, or None if the server is full."""
+        d = np.ascontiguousarray(np.asarray(desc, dtype=DESC_DTYPE).reshape(1))
+        t = ctypes.c_uint64()
+        st = lib().bi_server_submit(self._h, d.ctypes.data_as(ctypes.c_void_p), ctypes.byref(t))
+        if st == BI_EBUSY:
+            return None
+        _check(st)
+        return t.value
+
+    def poll(self, max_count: int = 4096) -> np.ndarray:
+        out = np.zeros(max_count, dtype=COMPLETION_DTYPE)
+        k = ctypes.c_uint32()
+        _check(lib().bi_server_poll(self._h, out.ctypes.data_as(ctypes.c_void_p), max_count, ctypes.byref(k)))
+        return out[: k.value]
+
+    def release(self, ticket: int):
+        _check(lib().bi_server_release(self._h, int(ticket)))
+
+    def info(self) -> dict:
+        v = (ctypes.c_uint64 * 10)()
+        _check(lib().bi_server_info(self._h, ctypes.cast(v, ctypes.c_void_p)))
+        keys = ("arena_ptr", "arena_limbs", "ctas", "smem_bytes", "launches", "busy", "lost", "ring_slots",
+                "submitted", "completed")
+        return dict(zip(keys, list(v)))
+
+    def replay(self, descs: np.ndarray, arrival_ns: np.ndarray):
+        """Open-loop replay; returns (latency_ns, completions, report)."""
+        descs = np.ascontiguousarray(descs, dtype=DESC_DTYPE)
+        arrival_ns = np.ascontiguousarray(arrival_ns, dtype=np.uint64)
+        n = len(descs)
+        lat = np.zeros(n, np.uint64)
+        done = np.zeros(n, COMPLETION_DTYPE)
+        rep = (ctypes.c_double * len(REPORT_KEYS))()
+        _check(lib().bi_server_replay(self._h, descs.ctypes.data_as(ctypes.c_void_p),
+                                      arrival_ns.ctypes.data_as(ctypes.c_void_p), n,
+                                      lat.ctypes.data_as(ctypes.c_void_p), done.ctypes.data_as(ctypes.c_void_p),
+                                      ctypes.cast(rep, ctypes.c_void_p)))
+        return lat, done, _report(rep)
+
+    def close(self):
+        if self._h:
+            lib().bi_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def replay_plain(operands, arena, descs: np.ndarray, arrival_ns: np.ndarray, streams: int = 1):
+    """The same open-loop stream with one library launch per request;
+    returns (latency_ns, completions, report)."""
+    descs = np.ascontiguousarray(descs, dtype=DESC_DTYPE)
+    arrival_ns = np.ascontiguousarray(arrival_ns, dtype=np.uint64)
+    n = len(descs)
+    lat = np.zeros(n, np.uint64)
+    done = np.zeros(n, COMPLETION_DTYPE)
+    rep = (ctypes.c_double * len(REPORT_KEYS))()
+    _check(lib().bi_serve_replay_plain(operands.data_ptr(), arena.data_ptr(), arena.numel(),
+                                       descs.ctypes.data_as(ctypes.c_void_p),
+                                       arrival_ns.ctypes.data_as(ctypes.c_void_p), n, streams,
+                                       lat.ctypes.data_as(ctypes.c_void_p), done.ctypes.data_as(ctypes.c_void_p),
+                                       ctypes.cast(rep, ctypes.c_void_p)))
+    return lat, done, _report(rep)
 
 
 # ---------------------------------------------------------------------------

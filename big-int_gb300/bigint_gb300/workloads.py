@@ -191,3 +191,58 @@ def uneven_batch(n: int = 100_000, seed: int = 1003, min_bits: int = 256, max_bi
     d["r2"] = r_off + rl
     d["flag"] = np.arange(n)
     return d, arena, int((rl + r2l).sum()), n
+
+
+# ---------------------------------------------------------------------------
+# serving stream: Poisson arrivals of add/sub/mul/div requests
+# ---------------------------------------------------------------------------
+
+SERVE_RATES = [10_000, 30_000, 100_000, 300_000, 1_000_000]   # offered requests/s
+
+
+def _unit(seed: int, n: int) -> np.ndarray:
+    return (splitmix64(seed, n) >> np.uint64(11)).astype(np.float64) / float(1 << 53)
+
+
+def serve_stream(n: int, rate: float, seed: int = 1004, pool_limbs: int = 1 << 22, min_bits: int = 512,
+                 max_bits: int = 32768, mix=(0.15, 0.15, 0.40, 0.30)):
+    """Requests and arrival times of the serving benchmark.
+
+    Operand sizes are log-uniform in [min_bits, max_bits] (m = ceil(bits/64)
+    64-bit limbs); the operation is add, sub, full multiply or division with
+    the probabilities `mix`; a division divides the drawn size by a divisor
+    of half as many limbs.  Operands are windows at even limb offsets of one
+    shared pool of `pool_limbs` random limbs (splitmix64 stream seed + 5,
+    resident on the device).  Arrivals form a Poisson process of `rate`
+    requests/s.  Returns (descs, arrival_ns, pool_seed).
+    """
+    from . import DESC_DTYPE, OP_ADD, OP_DIV, OP_MULFULL, OP_SUB
+
+    lo, hi = np.log2(min_bits), np.log2(max_bits)
+    bits = np.exp2(lo + (hi - lo) * _unit(seed, n))
+    m = np.maximum(1, np.ceil(bits / 64.0)).astype(np.int64)
+    sel = _unit(seed + 1, n)
+    c = np.cumsum(mix) / np.sum(mix)
+    op = np.where(sel < c[0], OP_ADD, np.where(sel < c[1], OP_SUB, np.where(sel < c[2], OP_MULFULL, OP_DIV)))
+    mb = np.where(op == OP_DIV, np.maximum(1, m // 2), m)
+    a = 2 * np.floor(_unit(seed + 2, n) * ((pool_limbs - m) // 2 + 1)).astype(np.int64)
+    b = 2 * np.floor(_unit(seed + 3, n) * ((pool_limbs - mb) // 2 + 1)).astype(np.int64)
+    gaps = -np.log1p(-_unit(seed + 4, n)) / float(rate)
+    arrival_ns = np.round(np.cumsum(gaps) * 1e9).astype(np.uint64)
+    d = np.zeros(n, dtype=DESC_DTYPE)
+    d["op"] = op
+    d["m"] = m
+    d["mb"] = mb
+    d["a"] = a
+    d["b"] = b
+    return d, arrival_ns, seed + 5
+
+
+def serve_pool_device(pool_limbs: int, pool_seed: int, device="cuda"):
+    import torch
+
+    from . import fill_splitmix64
+
+    t = torch.empty(pool_limbs, dtype=torch.int64, device=device)
+    fill_splitmix64(t, pool_seed, 0)
+    return t

@@ -232,6 +232,7 @@ const char* bi_status_string(bi_status s) {
     case BI_ETIMEDOUT: return "BI_ETIMEDOUT";
     case BI_ECUDA: return "BI_ECUDA";
     case BI_EUNSUPPORTED: return "BI_EUNSUPPORTED";
+    case BI_EBUSY: return "BI_EBUSY";
     default: return "BI_UNKNOWN";
     }
 }

@@ -45,6 +45,7 @@ typedef int bi_status;
 #define BI_ETIMEDOUT     4  /* a bounded device wait gave up */
 #define BI_ECUDA         5  /* a CUDA runtime call or launch failed */
 #define BI_EUNSUPPORTED  6  /* size beyond what this build supports */
+#define BI_EBUSY         7  /* serving loop full: retry after a poll/release */
 
 typedef void* bi_stream;
 
@@ -224,6 +225,77 @@ uint32_t bi_batch_noalloc_max_descs(void);
 bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count,
                                const uint64_t* in, uint64_t* out, uint8_t* flags,
                                bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
+/* Serving loop: requests of any operation and size, submitted one at a    */
+/* time, run by a persistent device-resident kernel with continuous        */
+/* batching.  No counterpart in the reference (its benchmarks launch fixed */
+/* batches, cuda/main.cu:476-515).  A request is a bi_desc over the        */
+/* server's operand arena `in` (device, 16-byte aligned); the server fills */
+/* in r, r2 (limb offsets of the results in its output arena) and ignores  */
+/* flag.  64-bit limbs; m <= max_limbs for every op (the dividend's limbs  */
+/* for BI_OP_DIV, divisor 1 <= mb <= m).                                   */
+/*                                                                         */
+/* Admission: a request enters when one of ring_slots slots and room for   */
+/* its results in the output arena (the HBM budget) are free; otherwise    */
+/* bi_server_submit returns BI_EBUSY and the caller polls, releases and    */
+/* retries.  Slots and arena space are reclaimed in submission order as    */
+/* requests are released.  The loop's CTAs leave after idle_us without a   */
+/* request and the next submit or poll relaunches it.  One client thread   */
+/* per server.  Results stay valid in the arena until released.            */
+/* ---------------------------------------------------------------------- */
+typedef struct bi_server bi_server;
+
+typedef struct bi_completion {
+    uint64_t ticket;    /* request number returned by bi_server_submit */
+    uint64_t r, r2;     /* limb offsets of the result(s) in the output arena */
+    uint32_t status;    /* sub: 1 if a < b; div: as bi_div_u64; 255: lost */
+    uint32_t op;
+} bi_completion;
+
+typedef struct bi_serve_report {
+    double requests;      /* requests completed */
+    double launches;      /* kernel launches: loop (re)starts, or one per request */
+    double busy;          /* admissions deferred for want of a slot or arena room */
+    double duration_s;    /* replay start to the last completion seen */
+    double offered_rps;   /* requests / last arrival time */
+    double achieved_rps;  /* requests / duration_s */
+    double p50_us, p90_us, p99_us, p999_us, max_us, mean_us;  /* arrival -> completion seen */
+} bi_serve_report;
+
+/* out == NULL: the server allocates an arena of out_limbs limbs (0: an    */
+/* eighth of the free HBM, at most 2^28 limbs).  ring_slots: power of two  */
+/* (0: 65536); max_limbs (0: 512, at most 2048) sizes the shared memory;   */
+/* ctas (0: as many as are resident at once); idle_us (0: 2000).           */
+bi_status bi_server_create(bi_server** server, const uint64_t* in, uint64_t in_limbs,
+                           uint64_t* out, uint64_t out_limbs, uint32_t ring_slots,
+                           uint32_t max_limbs, uint32_t ctas, uint32_t idle_us);
+bi_status bi_server_submit(bi_server* server, const bi_desc* request, uint64_t* ticket);
+/* Collect up to max completions (in completion order) into out.           */
+bi_status bi_server_poll(bi_server* server, bi_completion* out, uint32_t max, uint32_t* count);
+/* Return a completed request's slot and arena space.                      */
+bi_status bi_server_release(bi_server* server, uint64_t ticket);
+/* info[0..9] = arena pointer, arena limbs, CTAs, shared bytes per CTA,    */
+/* launches, deferred admissions, lost requests, ring slots, submitted,    */
+/* completed.                                                              */
+bi_status bi_server_info(const bi_server* server, uint64_t* info);
+/* Stops the loop (queued requests finish first) and frees the server.     */
+bi_status bi_server_destroy(bi_server* server);
+
+/* Open-loop replay on an idle server: request i arrives arrival_ns[i] ns  */
+/* after the start (non-decreasing), is admitted when it can be, and is    */
+/* released once its completion is seen; latency_ns[i] = completion seen - */
+/* arrival.  done (may be NULL) receives each request's completion.        */
+bi_status bi_server_replay(bi_server* server, const bi_desc* requests,
+                           const uint64_t* arrival_ns, uint64_t n, uint64_t* latency_ns,
+                           bi_completion* done, bi_serve_report* report);
+/* The same stream with one library launch per request (bi_add_u64, ...,  */
+/* bi_div_u64 with n = 1) round-robin over `streams` streams, each result  */
+/* placed in `out` in arrival order; completion seen by event query.        */
+bi_status bi_serve_replay_plain(const uint64_t* in, uint64_t* out, uint64_t out_limbs,
+                                const bi_desc* requests, const uint64_t* arrival_ns,
+                                uint64_t n, uint32_t streams, uint64_t* latency_ns,
+                                bi_completion* done, bi_serve_report* report);
 
 /* ---------------------------------------------------------------------- */
 /* Synthetic inputs: dst[i] = splitmix64 output number offset+i+1 of the   */

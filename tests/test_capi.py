@@ -74,3 +74,19 @@ def test_library_built_for_sm103a():
 
     assert "arch=compute_103a,code=sm_103a" in " ".join(B._build.ARCH)
     assert os.path.exists(B.LIB_PATH)
+
+
+def test_server_rejects_bad_arguments_on_host(L):
+    """The serving loop validates its arguments before any CUDA call."""
+    h = ctypes.c_void_p()
+    fake = ctypes.c_void_p(0x1000)
+    assert L.bi_server_create(ctypes.byref(h), None, 0, None, 0, 0, 0, 0, 0) == 1      # no operands
+    assert L.bi_server_create(None, fake, 16, None, 0, 0, 0, 0, 0) == 1                 # NULL handle
+    assert L.bi_server_create(ctypes.byref(h), ctypes.c_void_p(0x1008), 16, None, 0, 0, 0, 0, 0) == 1  # misaligned
+    assert L.bi_server_create(ctypes.byref(h), fake, 16, None, 0, 3, 0, 0, 0) == 1      # ring not a power of 2
+    assert L.bi_server_create(ctypes.byref(h), fake, 16, None, 0, 0, 4096, 0, 0) == 6   # max_limbs too large
+    assert not h.value
+    assert L.bi_server_submit(None, None, None) == 1
+    assert L.bi_server_poll(None, None, 0, None) == 1
+    assert L.bi_server_destroy(None) == 0
+    assert L.bi_status_string(7) == b"BI_EBUSY"
