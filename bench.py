@@ -671,10 +671,10 @@ def run_ours(args) -> None:
                          "frac": round(achieved / peak, 4),
                          "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "of fallback 6.8 TB/s",
-                         "kernel": "addsub_kernel (add and sub launches)", "bytes_per_launch": int(bytes_per_launch),
+                         "kernel": "addsub_chunk_kernel (add and sub launches)", "bytes_per_launch": int(bytes_per_launch),
                          "avg_launch_ms": round(avg_launch_ms, 5),
-                         "traffic": (ncu_traffic("addsub_kernel") or {}).get("bytes_per_launch"),
-                         "traffic_source": (ncu_traffic("addsub_kernel") or {}).get("source")},
+                         "traffic": (ncu_traffic("addsub_chunk_kernel") or {}).get("bytes_per_launch"),
+                         "traffic_source": (ncu_traffic("addsub_chunk_kernel") or {}).get("source")},
             "per_size_gbs": {k: round(3 * total * 8 / (float(np.mean(v)) / 1e3) / 1e9, 1) for k, v in per_launch.items()},
             "e2e": e2e,
             "gpu_launches": len(events),

@@ -152,9 +152,11 @@ static bool run_in_place(const HostIO& io, uint64_t n, Launch launch, bi_status*
     return true;
 }
 
-template <typename T, typename Launch>
+// `link` runs the in-place pass on pinned buffers, `launch` the staged
+// chunks in device memory.
+template <typename T, typename Launch, typename Link>
 static bi_status host_binary(const T* ha, const T* hb, T* hr, uint8_t* hsign, uint32_t m, uint64_t n,
-                             size_t out_limbs_per_inst, Launch launch) {
+                             size_t out_limbs_per_inst, Launch launch, Link link) {
     if (n == 0) return BI_OK;
     if (m == 0) return set_error(BI_EINVAL, "m must be >= 1");
     if (!ha || !hb || !hr) return set_error(BI_EINVAL, "NULL host buffer");
@@ -166,9 +168,18 @@ static bi_status host_binary(const T* ha, const T* hb, T* hr, uint8_t* hsign, ui
     auto fn = [&](void* da, void* db, void* dr, void*, uint8_t* ds, uint64_t cnt, cudaStream_t s) {
         return launch((const T*)da, (const T*)db, (T*)dr, ds, cnt, s);
     };
+    auto fn_link = [&](void* da, void* db, void* dr, void*, uint8_t* ds, uint64_t cnt, cudaStream_t s) {
+        return link((const T*)da, (const T*)db, (T*)dr, ds, cnt, s);
+    };
     bi_status rs;
-    if (run_in_place(io, n, fn, &rs)) return rs;
+    if (run_in_place(io, n, fn_link, &rs)) return rs;
     return host_pipelined(io, n, fn);
+}
+
+template <typename T, typename Launch>
+static bi_status host_binary(const T* ha, const T* hb, T* hr, uint8_t* hsign, uint32_t m, uint64_t n,
+                             size_t out_limbs_per_inst, Launch launch) {
+    return host_binary<T>(ha, hb, hr, hsign, m, n, out_limbs_per_inst, launch, launch);
 }
 
 template <typename T>
@@ -245,12 +256,18 @@ bi_status bi_host_add_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uin
     return host_binary<uint64_t>(a, b, r, nullptr, m, n, m,
         [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
             return bi_add_u64(da, db, dr, m, cnt, cs);
+        },
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return add_link_u64(da, db, dr, m, cnt, cs);
         });
 }
 bi_status bi_host_add_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n) {
     return host_binary<uint32_t>(a, b, r, nullptr, m, n, m,
         [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
             return bi_add_u32(da, db, dr, m, cnt, cs);
+        },
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t*, uint64_t cnt, cudaStream_t cs) {
+            return add_link_u32(da, db, dr, m, cnt, cs);
         });
 }
 bi_status bi_host_sub_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t* sign, uint32_t m,
@@ -258,6 +275,9 @@ bi_status bi_host_sub_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uin
     return host_binary<uint64_t>(a, b, r, sign, m, n, m,
         [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t* ds, uint64_t cnt, cudaStream_t cs) {
             return bi_sub_u64(da, db, dr, ds, m, cnt, cs);
+        },
+        [&](const uint64_t* da, const uint64_t* db, uint64_t* dr, uint8_t* ds, uint64_t cnt, cudaStream_t cs) {
+            return sub_link_u64(da, db, dr, ds, m, cnt, cs);
         });
 }
 bi_status bi_host_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* sign, uint32_t m,
@@ -265,6 +285,9 @@ bi_status bi_host_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uin
     return host_binary<uint32_t>(a, b, r, sign, m, n, m,
         [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t* ds, uint64_t cnt, cudaStream_t cs) {
             return bi_sub_u32(da, db, dr, ds, m, cnt, cs);
+        },
+        [&](const uint32_t* da, const uint32_t* db, uint32_t* dr, uint8_t* ds, uint64_t cnt, cudaStream_t cs) {
+            return sub_link_u32(da, db, dr, ds, m, cnt, cs);
         });
 }
 

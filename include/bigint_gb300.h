@@ -279,7 +279,9 @@ bi_status bi_server_release(bi_server* server, uint64_t ticket);
 /* launches, deferred admissions, lost requests, ring slots, submitted,    */
 /* completed.                                                              */
 bi_status bi_server_info(const bi_server* server, uint64_t* info);
-/* Stops the loop (queued requests finish first) and frees the server.     */
+/* Stops the loop and frees the server.  A running loop first finishes     */
+/* every request already submitted; requests submitted after the loop     */
+/* ended without a poll or submit to relaunch it are dropped.             */
 bi_status bi_server_destroy(bi_server* server);
 
 /* Open-loop replay on an idle server: request i arrives arrival_ns[i] ns  */

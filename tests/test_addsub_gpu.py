@@ -81,8 +81,10 @@ def test_max_size(bigint, oracle, dtype):
 
 @pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
 @pytest.mark.parametrize("m", [3, 16, 64, 513])
-def test_unaligned_buffers(bigint, oracle, dtype, m):
-    """Buffers offset by one limb take the scalar (non-16-byte) path."""
+@pytest.mark.parametrize("shift_bytes", [8, 16])
+def test_unaligned_buffers(bigint, oracle, dtype, m, shift_bytes):
+    """Buffers offset by 8 bytes take the scalar path; by 16 bytes, the
+    16-byte path even where m would allow the 64-byte-chunk path."""
     import torch
 
     B = bigint
@@ -90,12 +92,13 @@ def test_unaligned_buffers(bigint, oracle, dtype, m):
     a = uniform_limbs(5, n, m, dtype)
     b = uniform_limbs(6, n, m, dtype)
     wide = {np.uint64: torch.int64, np.uint32: torch.int32}[dtype]
-    da = torch.empty(n * m + 1, dtype=wide, device="cuda")
-    db = torch.empty(n * m + 1, dtype=wide, device="cuda")
-    dr = torch.empty(n * m + 1, dtype=wide, device="cuda")
-    da[1:] = B.to_device(a.reshape(-1))
-    db[1:] = B.to_device(b.reshape(-1))
-    A, Bt, R = da[1:].view(n, m), db[1:].view(n, m), dr[1:].view(n, m)
+    k = shift_bytes // np.dtype(dtype).itemsize
+    da = torch.empty(n * m + k, dtype=wide, device="cuda")
+    db = torch.empty(n * m + k, dtype=wide, device="cuda")
+    dr = torch.empty(n * m + k, dtype=wide, device="cuda")
+    da[k:] = B.to_device(a.reshape(-1))
+    db[k:] = B.to_device(b.reshape(-1))
+    A, Bt, R = da[k:].view(n, m), db[k:].view(n, m), dr[k:].view(n, m)
     B.add(A, Bt, out=R)
     assert (B.to_host(R.contiguous(), dtype) == oracle.add(a, b)).all()
     rs, sg = B.sub(A, Bt, out=R)
