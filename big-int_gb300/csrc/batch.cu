@@ -12,12 +12,15 @@
 //     size mix keeps the warps busy;
 //   * multiplications are bucketed by padded size; a persistent CTA takes a
 //     bucket item (as many instances as fit one CTA, mulcore.cuh);
-//   * divisions, most expensive first, go one per CTA to a persistent kernel
-//     (divcore.cuh).
-// The three persistent kernels run concurrently on forked streams; the fork,
-// the three launches, the counter reset and the join are captured once into a
-// CUDA graph and replayed by every bi_plan_execute.  Work is handed out with
-// one atomic counter per kernel (no waiting on other CTAs).
+//   * divisions go one per CTA to persistent kernels (divcore.cuh), one per
+//     size class of dividend -- under 64 limbs on 64-thread CTAs, under 256
+//     on 128-thread CTAs, the rest on 256-thread CTAs -- each sized for the
+//     shared memory of its own largest division, so small divisions run many
+//     CTAs per SM instead of one; most expensive first within a class.
+// The five persistent kernels run concurrently on forked streams; the fork,
+// the launches, the counter reset and the join are captured once into a CUDA
+// graph and replayed by every bi_plan_execute.  Work is handed out with one
+// atomic counter per kernel (no waiting on other CTAs).
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -118,7 +121,16 @@ batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
     }
 }
 
-__global__ void __launch_bounds__(BATCH_CTA, 2)
+// division size classes by dividend limbs: < 64, < 256, the rest
+constexpr int DIV_CLASSES = 3;
+constexpr int DIV_CLASS_THREADS[DIV_CLASSES] = {64, 128, 256};
+constexpr int PLAN_KERNELS = 2 + DIV_CLASSES;   // add/sub, multiply, one per division class
+
+static inline int div_class(uint32_t mu) { return mu < 64 ? 0 : mu < 256 ? 1 : 2; }
+
+// At most 128 registers a thread, so 512 / THREADS CTAs fit an SM's register file.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS)
 batch_div_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
                  uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
     extern __shared__ __align__(16) uint64_t smem[];
@@ -169,12 +181,13 @@ struct bi_plan {
     bi_desc* d_descs = nullptr;
     uint32_t* d_addsub = nullptr;
     uint32_t* d_mul = nullptr;
-    uint32_t* d_div = nullptr;
+    uint32_t* d_div = nullptr;          // division list: class 0, then 1, then 2
     MulItem* d_items = nullptr;
-    uint32_t* d_counters = nullptr;
+    uint32_t* d_counters = nullptr;     // add/sub, multiply, one per division class
     uint32_t n_addsub = 0, n_mul = 0, n_items = 0, n_div = 0;
-    uint32_t max_mul_Lp_full = 0, max_mul_Lp_trunc = 0, max_div_mu = 0, max_div_mv = 0;
-    size_t mul_smem = 0, div_smem = 0;
+    uint32_t div_off[DIV_CLASSES] = {}, n_divc[DIV_CLASSES] = {};
+    uint32_t max_mul_Lp_full = 0, max_mul_Lp_trunc = 0;
+    size_t mul_smem = 0, div_smem = 0, divc_smem[DIV_CLASSES] = {};
     BatchTune tune = {4, 2, 1};
     cudaGraphExec_t exec = nullptr;
     const void* g_in = nullptr;
@@ -182,8 +195,8 @@ struct bi_plan {
     void* g_flags = nullptr;
     BatchTune g_tune = {0, 0, 0};
     cudaStream_t cap = nullptr;
-    cudaStream_t side[3] = {};
-    cudaEvent_t ev_fork = nullptr, ev_join[3] = {};
+    cudaStream_t side[PLAN_KERNELS] = {};
+    cudaEvent_t ev_fork = nullptr, ev_join[PLAN_KERNELS] = {};
     std::mutex mu;
 };
 
@@ -204,21 +217,59 @@ static size_t mul_smem_for(const bi_plan* p, int ipc_div) {
     return best;
 }
 
+// Division order: by size class, then most expensive first.
+static bool div_before(const bi_desc& x, const bi_desc& y) {
+    const int cx = div_class(x.m), cy = div_class(y.m);
+    if (cx != cy) return cx < cy;
+    return (uint64_t)x.m * x.mb > (uint64_t)y.m * y.mb;
+}
+
+// Per-class offsets, counts and shared memory of a division list sorted by div_before.
+static void div_classes(bi_plan* p, const bi_desc* descs, const uint32_t* div, uint32_t n) {
+    p->div_smem = 0;
+    for (int c = 0; c < DIV_CLASSES; c++) {
+        p->div_off[c] = 0;
+        p->n_divc[c] = 0;
+        p->divc_smem[c] = 0;
+    }
+    for (uint32_t k = 0; k < n; k++) {
+        const bi_desc& d = descs[div[k]];
+        const int c = div_class(d.m);
+        if (p->n_divc[c]++ == 0) p->div_off[c] = k;
+        p->divc_smem[c] = std::max(p->divc_smem[c], div_smem_bytes(div_geom(d.m, d.mb, 8)));
+        p->div_smem = std::max(p->div_smem, p->divc_smem[c]);
+    }
+}
+
 enum { COMP_ADDSUB = 1, COMP_MUL = 2, COMP_DIV = 4, COMP_ALL = 7 };
 
 struct Launch3 {
-    unsigned grid[3];
-    size_t smem[3];
+    unsigned grid[PLAN_KERNELS];
+    size_t smem[PLAN_KERNELS];
 };
 
-// Grid sizes and shared memory of the three kernels for tuning t; sets the
+template <int THREADS>
+static bi_status prepare_div_class(uint32_t n, size_t smem, int sms, unsigned* grid) {
+    int occ = 1;
+    auto k = batch_div_kernel<THREADS>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, THREADS, smem) != cudaSuccess)
+        return set_error(BI_ECUDA, "batch div kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
+    *grid = (unsigned)std::min<uint64_t>(n, (uint64_t)sms * (occ < 1 ? 1 : occ));
+    return BI_OK;
+}
+
+// Grid sizes and shared memory of the kernels for tuning t; sets the
 // kernels' shared-memory limits (done outside any stream capture).
 static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
     const int sms = num_sms();
     L->grid[0] = (unsigned)std::min<uint64_t>((p->n_addsub + 7) / 8, (uint64_t)sms * 8);
     L->smem[0] = 0;
     L->smem[1] = mul_smem_for(p, t.mul_ipc_div);
-    L->smem[2] = p->div_smem;
+    for (int c = 0; c < DIV_CLASSES; c++) {
+        L->smem[2 + c] = p->divc_smem[c];
+        L->grid[2 + c] = 0;
+    }
     int occ = 1;
     if (p->n_items) {
         if (cudaFuncSetAttribute(batch_mul_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem[1]) != cudaSuccess ||
@@ -226,19 +277,17 @@ static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
             return set_error(BI_ECUDA, "batch mul kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
         L->grid[1] = (unsigned)std::min<uint64_t>(p->n_items, (uint64_t)sms * (occ < 1 ? 1 : occ));
     }
-    if (p->n_div) {
-        occ = 1;
-        if (cudaFuncSetAttribute(batch_div_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem[2]) != cudaSuccess ||
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_div_kernel, BATCH_CTA, L->smem[2]) != cudaSuccess)
-            return set_error(BI_ECUDA, "batch div kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
-        L->grid[2] = (unsigned)std::min<uint64_t>(p->n_div, (uint64_t)sms * (occ < 1 ? 1 : occ));
-    }
+    if (p->n_divc[0]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[0]>(p->n_divc[0], L->smem[2], sms, &L->grid[2]));
+    if (p->n_divc[1]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[1]>(p->n_divc[1], L->smem[3], sms, &L->grid[3]));
+    if (p->n_divc[2]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[2]>(p->n_divc[2], L->smem[4], sms, &L->grid[4]));
     return BI_OK;
 }
 
+// s[k] is the stream of kernel k (add/sub, multiply, division classes 0..2).
 static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags,
-                                     const BatchTune& t, const Launch3& L, cudaStream_t s_add,
-                                     cudaStream_t s_mul, cudaStream_t s_div, int comps = COMP_ALL) {
+                                     const BatchTune& t, const Launch3& L, const cudaStream_t* s,
+                                     int comps = COMP_ALL) {
+    cudaStream_t s_add = s[0], s_mul = s[1];
     if (p->n_addsub && (comps & COMP_ADDSUB)) {
         const unsigned grid = L.grid[0];
         if (t.addsub_vec == 2 && t.addsub_rows == 4)
@@ -256,16 +305,29 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
                                                                      p->d_counters + 1, in, out, t.mul_ipc_div);
         BI_RETURN_IF(check_launch("batch mul kernel"));
     }
-    if (p->n_div && (comps & COMP_DIV)) {
-        batch_div_kernel<<<L.grid[2], BATCH_CTA, L.smem[2], s_div>>>(p->d_descs, p->d_div, p->n_div,
-                                                                     p->d_counters + 2, in, out, flags);
-        BI_RETURN_IF(check_launch("batch div kernel"));
+    if (comps & COMP_DIV) {
+        // the largest class first: its divisions take longest
+        if (p->n_divc[2]) {
+            batch_div_kernel<DIV_CLASS_THREADS[2]><<<L.grid[4], DIV_CLASS_THREADS[2], L.smem[4], s[4]>>>(
+                p->d_descs, p->d_div + p->div_off[2], p->n_divc[2], p->d_counters + 4, in, out, flags);
+            BI_RETURN_IF(check_launch("batch div kernel"));
+        }
+        if (p->n_divc[1]) {
+            batch_div_kernel<DIV_CLASS_THREADS[1]><<<L.grid[3], DIV_CLASS_THREADS[1], L.smem[3], s[3]>>>(
+                p->d_descs, p->d_div + p->div_off[1], p->n_divc[1], p->d_counters + 3, in, out, flags);
+            BI_RETURN_IF(check_launch("batch div kernel"));
+        }
+        if (p->n_divc[0]) {
+            batch_div_kernel<DIV_CLASS_THREADS[0]><<<L.grid[2], DIV_CLASS_THREADS[0], L.smem[2], s[2]>>>(
+                p->d_descs, p->d_div + p->div_off[0], p->n_divc[0], p->d_counters + 2, in, out, flags);
+            BI_RETURN_IF(check_launch("batch div kernel"));
+        }
     }
     return BI_OK;
 }
 
-// Capture counter reset, fork, the three persistent kernels and the join
-// into one executable graph.
+// Capture counter reset, fork, the persistent kernels and the join into one
+// executable graph.
 static bi_status capture_plan(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags) {
     if (p->exec) {
         cudaGraphExecDestroy(p->exec);
@@ -276,11 +338,11 @@ static bi_status capture_plan(bi_plan* p, const uint64_t* in, uint64_t* out, uin
     cudaGraph_t graph = nullptr;
     cudaError_t e = cudaStreamBeginCapture(p->cap, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return set_error(BI_ECUDA, "plan capture: %s", cudaGetErrorString(e));
-    cudaMemsetAsync(p->d_counters, 0, 3 * sizeof(uint32_t), p->cap);
+    cudaMemsetAsync(p->d_counters, 0, PLAN_KERNELS * sizeof(uint32_t), p->cap);
     cudaEventRecord(p->ev_fork, p->cap);
-    for (int k = 0; k < 3; k++) cudaStreamWaitEvent(p->side[k], p->ev_fork, 0);
-    bi_status st = launch_plan_kernels(p, in, out, flags, p->tune, L, p->side[0], p->side[1], p->side[2]);
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < PLAN_KERNELS; k++) cudaStreamWaitEvent(p->side[k], p->ev_fork, 0);
+    bi_status st = launch_plan_kernels(p, in, out, flags, p->tune, L, p->side);
+    for (int k = 0; k < PLAN_KERNELS; k++) {
         cudaEventRecord(p->ev_join[k], p->side[k]);
         cudaStreamWaitEvent(p->cap, p->ev_join[k], 0);
     }
@@ -312,7 +374,7 @@ static void plan_free(bi_plan* p) {
     cudaFree(p->d_div);
     cudaFree(p->d_items);
     cudaFree(p->d_counters);
-    for (int k = 0; k < 3; k++) {
+    for (int k = 0; k < PLAN_KERNELS; k++) {
         if (p->side[k]) cudaStreamDestroy(p->side[k]);
         if (p->ev_join[k]) cudaEventDestroy(p->ev_join[k]);
     }
@@ -361,8 +423,6 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
                 plan_free(p);
                 return set_error(BI_EINVAL, "descriptor %llu: need 1 <= mb <= m", (unsigned long long)i);
             }
-            p->max_div_mu = std::max(p->max_div_mu, d.m);
-            p->max_div_mv = std::max(p->max_div_mv, d.mb);
             div.push_back((uint32_t)i);
             break;
         default:
@@ -372,9 +432,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     }
     // largest first: long instances start early, short ones fill the tail
     std::stable_sort(addsub.begin(), addsub.end(), [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
-    std::stable_sort(div.begin(), div.end(), [&](uint32_t x, uint32_t y) {
-        return (uint64_t)descs[x].m * descs[x].mb > (uint64_t)descs[y].m * descs[y].mb;
-    });
+    std::stable_sort(div.begin(), div.end(), [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y]); });
     std::stable_sort(mulkeys.begin(), mulkeys.end(), [](const std::pair<uint64_t, uint32_t>& x,
                                                         const std::pair<uint64_t, uint32_t>& y) {
         return x.first > y.first;
@@ -402,15 +460,15 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     p->n_mul = (uint32_t)mul.size();
     p->n_items = (uint32_t)items.size();
     p->n_div = (uint32_t)div.size();
-    if (p->n_div) p->div_smem = div_smem_bytes(div_geom(p->max_div_mu, p->max_div_mv, 8));
+    div_classes(p, descs, div.data(), p->n_div);
     if (p->div_smem > 227 * 1024 || mul_smem_for(p, 1) > 227 * 1024) {
         plan_free(p);
         return set_error(BI_EUNSUPPORTED, "batch sizes need too much shared memory");
     }
     cudaError_t e = cudaStreamCreateWithFlags(&p->cap, cudaStreamNonBlocking);
-    for (int k = 0; k < 3 && e == cudaSuccess; k++) e = cudaStreamCreateWithFlags(&p->side[k], cudaStreamNonBlocking);
+    for (int k = 0; k < PLAN_KERNELS && e == cudaSuccess; k++) e = cudaStreamCreateWithFlags(&p->side[k], cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&p->ev_fork, cudaEventDisableTiming);
-    for (int k = 0; k < 3 && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&p->ev_join[k], cudaEventDisableTiming);
+    for (int k = 0; k < PLAN_KERNELS && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&p->ev_join[k], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         plan_free(p);
         return set_error(BI_ECUDA, "plan streams: %s", cudaGetErrorString(e));
@@ -422,7 +480,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     if (st == BI_OK) st = dev_upload(&p->d_div, div, p->cap);
     if (st == BI_OK) st = dev_upload(&p->d_items, items, p->cap);
     if (st == BI_OK) {
-        std::vector<uint32_t> zeros(4, 0);
+        std::vector<uint32_t> zeros(8, 0);
         st = dev_upload(&p->d_counters, zeros, p->cap);
     }
     if (st == BI_OK && cudaStreamSynchronize(p->cap) != cudaSuccess) st = set_error(BI_ECUDA, "plan upload failed");
@@ -470,9 +528,10 @@ static float time_component(bi_plan* p, const uint64_t* in, uint64_t* out, uint8
     Launch3 L;
     if (prepare_launch(p, t, &L) != BI_OK) return 1e30f;
     for (int r = 0; r < reps + 1; r++) {
-        cudaMemsetAsync(p->d_counters, 0, 3 * sizeof(uint32_t), p->cap);
+        cudaMemsetAsync(p->d_counters, 0, PLAN_KERNELS * sizeof(uint32_t), p->cap);
         cudaEventRecord(e0, p->cap);
-        bi_status st = launch_plan_kernels(p, in, out, flags, t, L, p->cap, p->cap, p->cap, comp);
+        const cudaStream_t ss[PLAN_KERNELS] = {p->cap, p->cap, p->cap, p->cap, p->cap};
+        bi_status st = launch_plan_kernels(p, in, out, flags, t, L, ss, comp);
         cudaEventRecord(e1, p->cap);
         cudaEventSynchronize(e1);
         float ms = 0;
@@ -640,17 +699,13 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
             na_keys[nk++] = {((uint64_t)full << 40) | ((uint64_t)Lp << 8), (uint32_t)i};
         } else if (d.op == BI_OP_DIV) {
             if (d.mb == 0 || d.mb > d.m) return set_error(BI_EINVAL, "descriptor %llu: need 1 <= mb <= m", (unsigned long long)i);
-            p.max_div_mu = std::max(p.max_div_mu, d.m);
-            p.max_div_mv = std::max(p.max_div_mv, d.mb);
             na_div[nd++] = (uint32_t)i;
         } else {
             return set_error(BI_EINVAL, "descriptor %llu: unknown op %u", (unsigned long long)i, d.op);
         }
     }
     std::stable_sort(na_add, na_add + na, [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
-    std::stable_sort(na_div, na_div + nd, [&](uint32_t x, uint32_t y) {
-        return (uint64_t)descs[x].m * descs[x].mb > (uint64_t)descs[y].m * descs[y].mb;
-    });
+    std::stable_sort(na_div, na_div + nd, [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y]); });
     std::stable_sort(na_keys, na_keys + nk, [](const std::pair<uint64_t, uint32_t>& x,
                                                const std::pair<uint64_t, uint32_t>& y) { return x.first > y.first; });
     for (uint32_t k = 0; k < nk;) {
@@ -675,7 +730,7 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
     p.n_mul = nm;
     p.n_items = ni;
     p.n_div = nd;
-    if (nd) p.div_smem = div_smem_bytes(div_geom(p.max_div_mu, p.max_div_mv, 8));
+    div_classes(&p, descs, na_div, nd);
     if (p.div_smem > 227 * 1024 || mul_smem_for(&p, 1) > 227 * 1024)
         return set_error(BI_EUNSUPPORTED, "batch sizes need too much shared memory");
     p.d_descs = (bi_desc*)(base + NA_DESC_OFF);
@@ -693,14 +748,15 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
     if (e == cudaSuccess && nm) e = cudaMemcpyAsync(p.d_mul, na_mul, nm * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && nd) e = cudaMemcpyAsync(p.d_div, na_div, nd * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && ni) e = cudaMemcpyAsync(p.d_items, na_items, ni * sizeof(MulItem), cudaMemcpyHostToDevice, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p.d_counters, 0, 3 * sizeof(uint32_t), s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.d_counters, 0, PLAN_KERNELS * sizeof(uint32_t), s);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_error(BI_ECUDA, "staging the batch: %s", cudaGetErrorString(e));
     }
     Launch3 L;
     BI_RETURN_IF(prepare_launch(&p, p.tune, &L));
-    BI_RETURN_IF(launch_plan_kernels(&p, in, out, flags, p.tune, L, s, s, s));
+    const cudaStream_t ss[PLAN_KERNELS] = {s, s, s, s, s};
+    BI_RETURN_IF(launch_plan_kernels(&p, in, out, flags, p.tune, L, ss));
     // the host staging arrays may be reused once the copies have read them
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return set_error(BI_ECUDA, "batch run: %s", cudaGetErrorString(e));

@@ -155,56 +155,110 @@ __device__ __forceinline__ int block_cmp(const uint64_t* X, int lx, const uint64
     return (m & 1u) ? 1 : -1;
 }
 
-// out[0..olen) = (A[0..la) * Bm[0..lb)) mod B^olen, exact.  out must not
-// alias A, Bm or wbuf; wbuf holds ceil(olen/8)*10 limbs.  Column windows of
-// 8 limbs are accumulated with row_mac8 (as in mul.cu) and merged with a
-// carry lookahead across windows.
+// R[0..10) += O[0..10) with the carry chain.
+__device__ __forceinline__ void add10(uint64_t (&R)[10], const uint64_t (&O)[10]) {
+    asm("add.cc.u64 %0, %0, %10;\n\taddc.cc.u64 %1, %1, %11;\n\taddc.cc.u64 %2, %2, %12;\n\t"
+        "addc.cc.u64 %3, %3, %13;\n\taddc.cc.u64 %4, %4, %14;\n\taddc.cc.u64 %5, %5, %15;\n\t"
+        "addc.cc.u64 %6, %6, %16;\n\taddc.cc.u64 %7, %7, %17;\n\taddc.cc.u64 %8, %8, %18;\n\t"
+        "addc.u64 %9, %9, %19;"
+        : "+l"(R[0]), "+l"(R[1]), "+l"(R[2]), "+l"(R[3]), "+l"(R[4]), "+l"(R[5]), "+l"(R[6]), "+l"(R[7]),
+          "+l"(R[8]), "+l"(R[9])
+        : "l"(O[0]), "l"(O[1]), "l"(O[2]), "l"(O[3]), "l"(O[4]), "l"(O[5]), "l"(O[6]), "l"(O[7]), "l"(O[8]),
+          "l"(O[9]));
+}
+
+// out[c..olen) for c >= floor(c_lo / 8) * 8: the limbs of (A[0..la) *
+// Bm[0..lb)) mod B^olen, exact when c_lo = 0.  With c_lo > 0 only the column
+// windows from floor(c_lo / 8) up are summed (a short product): the limbs
+// below are not written, and the value of out above c_lo falls short of the
+// true product's by less than min(la, lb) * B^(c_lo + 1) -- under one unit
+// two limbs above c_lo.  out must not alias A, Bm or wbuf; wbuf holds
+// ceil(olen/8)*10 limbs.
+//
+// Column windows of 8 limbs are accumulated with row_mac8 (as in mul.cu).  The
+// rows of each window are cut into S slices (S a power of two up to 32, the
+// one that minimises rounds x rows per slice for the CTA's size), computed by
+// S consecutive lanes and summed with warp shuffles, so a product with few
+// windows still occupies the CTA.  The windows are then merged with a carry
+// lookahead across windows.
 __device__ __forceinline__ void block_mul(const uint64_t* A, int la, const uint64_t* Bm, int lb, uint64_t* out,
-                                          int olen, uint64_t* wbuf, uint32_t* scratch) {
+                                          int olen, uint64_t* wbuf, uint32_t* scratch, int c_lo = 0) {
     constexpr int C = 8;
-    const int T = blockDim.x, t = threadIdx.x;
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31;
     const int W = (olen + C - 1) / C;
-    for (int w = t; w < W; w += T) {
-        const int k0 = w * C;
-        int ilo = k0 - lb + 1;
-        if (ilo < 0) ilo = 0;
-        int ihi = k0 + C;
-        if (ihi > la) ihi = la;
+    const int w0 = c_lo / C < W ? c_lo / C : W;
+    const int NW = W - w0;
+    int S = 1, lgS = 0;
+    const int mr = la < lb + C - 1 ? la : lb + C - 1;   // most rows of any window
+    if (NW < T && mr > C) {
+        uint32_t best = 0xffffffffu;
+        for (int lg = 0; lg <= 5; lg++) {
+            const uint32_t rounds = ((uint32_t)(NW << lg) + T - 1) / (uint32_t)T;
+            const uint32_t rows = (uint32_t)((((mr + (1 << lg) - 1) >> lg) + C - 1) & ~(C - 1));
+            const uint32_t cost = rounds * (rows + lg);
+            if (cost < best) { best = cost; S = 1 << lg; lgS = lg; }
+        }
+    }
+    for (int base = t & ~31; base < NW * S; base += T) {
+        const int j = base + lane;
+        const int w = w0 + (j >> lgS), sl = j & (S - 1);
         uint64_t R[C + 2];
 #pragma unroll
         for (int e = 0; e < C + 2; e++) R[e] = 0;
-        for (int i0 = ilo; i0 < ihi; i0 += C) {
-            uint64_t av[C], ext[2 * C];
+        if (j < NW * S) {
+            const int k0 = w * C;
+            int ilo = k0 - lb + 1;
+            if (ilo < 0) ilo = 0;
+            int ihi = k0 + C;
+            if (ihi > la) ihi = la;
+            const int len = ihi > ilo ? ihi - ilo : 0;
+            const int span = (((len + S - 1) >> lgS) + C - 1) & ~(C - 1);
+            const int lo = ilo + sl * span;
+            const int hi = lo + span < ihi ? lo + span : ihi;
+            for (int i0 = lo; i0 < hi; i0 += C) {
+                uint64_t av[C], ext[2 * C];
 #pragma unroll
-            for (int k = 0; k < C; k++) av[k] = (i0 + k < ihi) ? A[i0 + k] : 0;
+                for (int k = 0; k < C; k++) av[k] = (i0 + k < hi) ? A[i0 + k] : 0;
 #pragma unroll
-            for (int q = 0; q < 2 * C; q++) {
-                const int bi = k0 - i0 - C + q;
-                ext[q] = (bi >= 0 && bi < lb) ? Bm[bi] : 0;
+                for (int q = 0; q < 2 * C; q++) {
+                    const int bi = k0 - i0 - C + q;
+                    ext[q] = (bi >= 0 && bi < lb) ? Bm[bi] : 0;
+                }
+                // rows past hi are zero: skip them (each row extends R's carry chain)
+                const int nr = hi - i0;
+                row_mac8<8>(R, av[0], ext);
+                if (nr > 1) row_mac8<7>(R, av[1], ext);
+                if (nr > 2) row_mac8<6>(R, av[2], ext);
+                if (nr > 3) row_mac8<5>(R, av[3], ext);
+                if (nr > 4) row_mac8<4>(R, av[4], ext);
+                if (nr > 5) row_mac8<3>(R, av[5], ext);
+                if (nr > 6) row_mac8<2>(R, av[6], ext);
+                if (nr > 7) row_mac8<1>(R, av[7], ext);
             }
-            row_mac8<8>(R, av[0], ext);
-            row_mac8<7>(R, av[1], ext);
-            row_mac8<6>(R, av[2], ext);
-            row_mac8<5>(R, av[3], ext);
-            row_mac8<4>(R, av[4], ext);
-            row_mac8<3>(R, av[5], ext);
-            row_mac8<2>(R, av[6], ext);
-            row_mac8<1>(R, av[7], ext);
         }
+        // sum the S slices of a window (consecutive lanes) onto its slice 0
+        for (int off = S >> 1; off > 0; off >>= 1) {
+            uint64_t o[C + 2];
 #pragma unroll
-        for (int e = 0; e < C + 2; e++) wbuf[w * (C + 2) + e] = R[e];
+            for (int e = 0; e < C + 2; e++) o[e] = __shfl_down_sync(0xffffffffu, R[e], off);
+            if (sl < off) add10(R, o);
+        }
+        if (j < NW * S && sl == 0) {
+#pragma unroll
+            for (int e = 0; e < C + 2; e++) wbuf[w * (C + 2) + e] = R[e];
+        }
     }
     __syncthreads();
     // merge: thread takes windows [u_lo, u_hi); D_u = P_u + O_{u-1} (in place in wbuf)
-    const int cw = (W + T - 1) / T;
-    int u_lo = t * cw, u_hi = u_lo + cw;
+    const int cw = (NW + T - 1) / T;
+    int u_lo = w0 + t * cw, u_hi = u_lo + cw;
     if (u_lo > W) u_lo = W;
     if (u_hi > W) u_hi = W;
     uint32_t G = 0, P = 1;
-    uint32_t gs = 0, ps = 0;   // per-window bits (cw <= 32 assumed: W <= 32 * T)
+    uint32_t gs = 0, ps = 0;   // per-window bits (cw <= 32 assumed: NW <= 32 * T)
     for (int u = u_lo; u < u_hi; u++) {
         uint64_t o0 = 0, o1 = 0;
-        if (u > 0) {
+        if (u > w0) {
             o0 = wbuf[(u - 1) * (C + 2) + C];
             o1 = wbuf[(u - 1) * (C + 2) + C + 1];
         }
@@ -230,7 +284,7 @@ __device__ __forceinline__ void block_mul(const uint64_t* A, int la, const uint6
     uint32_t c_win = cin;
     for (int u = u_lo; u < u_hi; u++) {
         uint64_t o0 = 0, o1 = 0;
-        if (u > 0) {
+        if (u > w0) {
             o0 = wbuf[(u - 1) * (C + 2) + C];
             o1 = wbuf[(u - 1) * (C + 2) + C + 1];
         }

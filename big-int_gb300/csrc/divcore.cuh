@@ -115,8 +115,9 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
         block_mul(Vs, sl, Yp, p + 1, Tb, sl + 1, Wb, scratch);
         const bool e_neg = (Tb[sl] >> 63) == 0;    // T small: E = -T
         if (!e_neg) block_addsub(Tb, nullptr, 0, Tb, sl + 1, sl + 1, true, scratch);   // |E| = -T
-        // D = floor(Y_p * |E| / B^(2p+1))
-        block_mul(Yp, p + 1, Tb, sl + 1, Pr, p + sl + 2, Wb, scratch);
+        // D = floor(Y_p * |E| / B^(2p+1)), from a short product (columns >= 2p-1):
+        // at most one unit short, which the next step's residual absorbs
+        block_mul(Yp, p + 1, Tb, sl + 1, Pr, p + sl + 2, Wb, scratch, 2 * p - 1);
         const uint64_t* D = Pr + 2 * p + 1;
         const int Dlen = sl - p + 1;
         // Y_pn = Y_p * B^(pn-p) +/- D
@@ -128,13 +129,14 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
     }
     const uint64_t* Y = Yb + (Pmax - P);
 
-    // ---- quotient estimate: floor(Un * Y / B^(P+K))
+    // ---- quotient estimate: floor(Un * Y / B^(P+K)) from a short product
+    // (columns >= P+K-2): at most one short, corrected below with the rest
     uint64_t* Big = X + g.oBig;
     uint64_t* Qb = X + g.oQ;
     uint64_t* QV = X + g.oQV;
     uint64_t* Rb = X + g.oR;
     uint64_t* W2 = X + g.oW2;
-    block_mul(Un, H, Y, P + 1, Big, H + P + 1, W2, scratch);
+    block_mul(Un, H, Y, P + 1, Big, H + P + 1, W2, scratch, P + K - 2);
     for (int i = threadIdx.x; i < Qlen + 1; i += blockDim.x) Qb[i] = i < Qlen ? Big[P + K + i] : 0;
     __syncthreads();
 
