@@ -356,7 +356,8 @@ def measure_uneven_batch(B, L, stream, n: int = 100_000):
             "note": "one CUDA-graph replay of three concurrent persistent kernels vs one plain launch per (op, m) group"}
 
 
-def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100_000, streams: int = 4):
+def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100_000, streams: int = 4,
+                    saturation_rates=(2_000_000, 4_000_000)):
     """Poisson streams of requests (sizes log-uniform 512..32768 bits; 15% add,
     15% sub, 40% full multiply, 30% division; operands resident in a 2^24-limb
     device pool; a 2^26-limb result arena as the HBM budget): the
@@ -383,6 +384,7 @@ def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100
         return {k: (round(rep[k], 2) if isinstance(rep[k], float) else rep[k]) for k in keep}
 
     out = {}
+    beyond = {}
     with B.Server(pool, arena) as srv:
         info = srv.info()
         srv.replay(warm[0], warm[1])
@@ -390,6 +392,11 @@ def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100
             d, arr, _ = streams_of[r]
             _, _, rep = srv.replay(d, arr)
             out[str(r)] = {"loop": short(rep)}
+        # past the offered loads: where the loop saturates
+        for r in saturation_rates:
+            d, arr, _ = serve_stream(max_requests, r, seed=1005, pool_limbs=pool_limbs)
+            _, _, rep = srv.replay(d, arr)
+            beyond[str(r)] = short(rep)
     # the loop has stopped: the per-request launches get the whole GPU
     B.replay_plain(pool, arena, warm[0], warm[1], streams=streams)
     for r in rates:
@@ -400,7 +407,8 @@ def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100
         out[str(r)]["p99_ratio_launch_over_loop"] = round(pl["p99_us"] / lo["p99_us"], 2) if lo["p99_us"] else None
     del pool, arena
     torch.cuda.empty_cache()
-    return {"rates_rps": out, "loop_ctas": info["ctas"], "loop_smem_bytes": info["smem_bytes"],
+    return {"rates_rps": out, "loop_beyond_offered_loads": beyond, "loop_ctas": info["ctas"],
+            "loop_smem_bytes": info["smem_bytes"],
             "result_arena_limbs": info["arena_limbs"], "per_request_streams": streams,
             "note": "open-loop Poisson replay; latency = completion seen by the host - scheduled arrival"}
 

@@ -15,12 +15,14 @@
 // size and operation overlap on the device with no batch boundary, and the
 // host never launches a kernel per request.
 //
-// Every device wait is bounded by the global timer: a CTA that has seen no
-// request for idle_us leaves the loop (a host stop flag ends it as soon as the
-// CTA is idle); the last CTA to leave records the launch's epoch in mapped
-// memory, and the host relaunches the kernel when it holds unclaimed requests
-// and the loop has ended.  The wait for a claimed slot's contents gives up
-// after a second and completes the request with status 0xFF.
+// Every device wait is bounded by the global timer.  The loop ends as a whole:
+// when no CTA has claimed a request for idle_us (or the host's stop flag is
+// set), the first CTA to notice marks the launch closing and every CTA leaves
+// after its current request, so a launch never lingers with a few CTAs.  The
+// last CTA to leave records the launch's epoch in mapped memory, and the host
+// relaunches the kernel when it holds unclaimed requests and the loop has
+// ended.  The wait for a claimed slot's contents gives up after a second and
+// completes the request with status 0xFF.
 //
 // The driver functions at the end replay a timed arrival stream open-loop,
 // through the server and through one library launch per request, and report
@@ -63,8 +65,20 @@ struct ServeCtl {                      // mapped host memory
 struct ServeDev {                      // device memory
     unsigned long long head;           // requests claimed
     unsigned long long cq_pos;         // completion-queue positions handed out
+    unsigned long long tail_seen;      // the host tail as last read by some CTA
+    unsigned long long poll_ns;        // when some CTA last read the host tail
+    unsigned long long last_work;      // when some CTA last claimed a request (or started)
+    unsigned long long closing;        // epoch of a launch whose CTAs are to leave
     unsigned int left;                 // CTAs of the running launch that have left
+    unsigned int stop_seen;            // the host stop flag as last read
 };
+
+// Idle CTAs read the host-written tail and stop flag at most once per
+// SERVE_POLL_NS between them (one CTA wins a compare-and-swap on poll_ns and
+// refreshes tail_seen and stop_seen); the others read the copies in device
+// memory, so the line the host writes on every publish is not read by every
+// CTA.
+constexpr uint64_t SERVE_POLL_NS = 256;
 
 struct ServeArgs {
     const ServeSlot* slots;
@@ -103,25 +117,50 @@ __device__ __forceinline__ uint64_t global_ns() {
 enum : int { CLAIM_OK = 0, CLAIM_EXIT = 1, CLAIM_LOST = 2 };
 
 // Thread 0 of a CTA: claim the next published request.  Returns CLAIM_EXIT
-// after idle_ns without seeing a request (or at once when stop is set and
-// nothing is waiting), CLAIM_LOST if the claimed slot did not show the
-// request within SERVE_WAIT_NS.
+// once the launch is closing -- no CTA claimed a request for idle_ns, or
+// stop is set and nothing is waiting -- and CLAIM_LOST if the claimed slot
+// did not show the request within SERVE_WAIT_NS.
 __device__ int serve_claim(const ServeArgs& A, uint64_t& seq, bi_desc& d) {
     volatile unsigned long long* head = &A.dev->head;
-    uint64_t idle_since = global_ns();
+    volatile unsigned long long* seen = &A.dev->tail_seen;
+    volatile unsigned long long* polled = &A.dev->poll_ns;
+    volatile unsigned long long* last_work = &A.dev->last_work;
+    volatile unsigned long long* closing = &A.dev->closing;
     uint32_t nap = 32;
     uint64_t h;
     for (;;) {
+        if (*closing == A.epoch) return CLAIM_EXIT;
         h = *head;
-        const uint64_t t = ld_acquire_sys(&A.ctl->tail);
+        uint64_t t = *seen;
+        if (h >= t) {
+            const uint64_t now = global_ns(), last = *polled;
+            if (now - last >= SERVE_POLL_NS && atomicCAS(&A.dev->poll_ns, last, now) == last) {
+                const uint64_t ht = ld_acquire_sys(&A.ctl->tail);
+                if (ht > t) {
+                    atomicMax(&A.dev->tail_seen, ht);
+                    t = ht;
+                }
+                if (ld_relaxed_sys(&A.ctl->stop)) atomicExch(&A.dev->stop_seen, 1u);
+            }
+        }
         if (h < t) {
-            if (atomicCAS(&A.dev->head, h, h + 1) == h) break;
-            idle_since = global_ns();   // requests are waiting: not idle
+            if (atomicCAS(&A.dev->head, h, h + 1) == h) {
+                atomicMax(&A.dev->last_work, global_ns());
+                break;
+            }
             nap = 32;
             continue;
         }
-        if (ld_relaxed_sys(&A.ctl->stop)) return CLAIM_EXIT;
-        if (global_ns() - idle_since > A.idle_ns) return CLAIM_EXIT;
+        if (*(volatile unsigned int*)&A.dev->stop_seen || global_ns() - *last_work > A.idle_ns) {
+            // close only if the host has published nothing beyond what was claimed
+            const uint64_t ht = ld_acquire_sys(&A.ctl->tail);
+            if (ht > h) {
+                atomicMax(&A.dev->tail_seen, ht);
+                continue;
+            }
+            atomicExch(&A.dev->closing, A.epoch);   // every CTA of this launch leaves
+            return CLAIM_EXIT;
+        }
         __nanosleep(nap);
         if (nap < 1024) nap *= 2;
     }
@@ -156,6 +195,7 @@ __global__ void __launch_bounds__(SERVE_CTA, 2) serve_kernel(const ServeArgs A) 
     __shared__ int s_cmd;
     __shared__ uint32_t s_flag;
     __shared__ uint8_t s_sign;
+    if (threadIdx.x == 0) atomicMax(&A.dev->last_work, global_ns());   // a launch starts busy
     for (;;) {
         if (threadIdx.x == 0) {
             s_flag = 0;
@@ -343,10 +383,9 @@ static bi_status server_kick(bi_server* s) {
 
 static void server_publish(bi_server* s) { __atomic_store_n(&s->ctl->tail, s->published, __ATOMIC_RELEASE); }
 
-// Admit one request into the ring without publishing it.  BI_EBUSY: no slot
-// or no arena room until earlier requests are released.
-static bi_status server_admit(bi_server* s, const bi_desc* req, uint64_t* ticket) {
-    bi_desc d = *req;
+// The checks every request must pass before it is admitted.
+static bi_status server_validate(const bi_server* s, const bi_desc& req) {
+    bi_desc d = req;
     if (d.op > BI_OP_DIV) return set_error(BI_EINVAL, "serve: unknown op %u", d.op);
     if (d.op != BI_OP_DIV) d.mb = d.m;
     if (d.m == 0 || d.m > s->max_limbs)
@@ -355,12 +394,20 @@ static bi_status server_admit(bi_server* s, const bi_desc* req, uint64_t* ticket
     if (d.a > s->in_limbs || d.m > s->in_limbs - d.a || d.b > s->in_limbs || d.mb > s->in_limbs - d.b)
         return set_error(BI_EINVAL, "serve: operand outside the operand arena");
     if (request_smem(d) > s->smem) return set_error(BI_EUNSUPPORTED, "serve: request needs more shared memory than the loop holds");
+    if (((result_limbs(d) + 1) & ~1ull) > s->out_limbs) return set_error(BI_EINVAL, "serve: result larger than the output arena");
+    return BI_OK;
+}
+
+// Admit one validated request into the ring without publishing it.
+// BI_EBUSY: no slot or no arena room until earlier requests are released.
+static bi_status server_admit(bi_server* s, const bi_desc* req, uint64_t* ticket) {
+    bi_desc d = *req;
+    if (d.op != BI_OP_DIV) d.mb = d.m;
     if (s->published - s->released >= s->S) {
         s->busy++;
         return BI_EBUSY;
     }
     const uint64_t need = (result_limbs(d) + 1) & ~1ull;
-    if (need > s->out_limbs) return set_error(BI_EINVAL, "serve: result larger than the output arena");
     const uint64_t pos = s->alloc_head % s->out_limbs;
     const uint64_t skip = pos + need > s->out_limbs ? s->out_limbs - pos : 0;
     if (s->alloc_head + skip + need - s->alloc_tail > s->out_limbs) {
@@ -521,6 +568,7 @@ bi_status bi_server_create(bi_server** server, const uint64_t* in, uint64_t in_l
 
 bi_status bi_server_submit(bi_server* s, const bi_desc* req, uint64_t* ticket) {
     if (!s || !req) return set_error(BI_EINVAL, "serve: NULL argument");
+    BI_RETURN_IF(server_validate(s, *req));
     const bi_status st = server_admit(s, req, ticket);
     if (st != BI_OK) return st;
     server_publish(s);
@@ -563,8 +611,10 @@ bi_status bi_server_destroy(bi_server* s) {
 bi_status bi_server_replay(bi_server* s, const bi_desc* reqs, const uint64_t* arrival_ns, uint64_t n,
                            uint64_t* latency_ns, bi_completion* done, bi_serve_report* rep) {
     if (!s || (n && (!reqs || !arrival_ns || !latency_ns))) return set_error(BI_EINVAL, "serve: NULL argument");
-    for (uint64_t i = 1; i < n; i++)
-        if (arrival_ns[i] < arrival_ns[i - 1]) return set_error(BI_EINVAL, "serve: arrival times must not decrease");
+    for (uint64_t i = 0; i < n; i++) {
+        if (i && arrival_ns[i] < arrival_ns[i - 1]) return set_error(BI_EINVAL, "serve: arrival times must not decrease");
+        BI_RETURN_IF(server_validate(s, reqs[i]));
+    }
     const uint64_t seq0 = s->published, launches0 = s->launches, busy0 = s->busy;
     if (s->published != s->released) return set_error(BI_EINVAL, "serve: replay needs an idle server");
     std::vector<bi_completion> buf(4096);
