@@ -245,6 +245,41 @@ def run_reference(args) -> None:
 # GPU measurements
 # ---------------------------------------------------------------------------
 
+def div_limb_products(mu: int, mv: int) -> int:
+    """64x64-bit limb products in the multiplications one division performs
+    (the shifted-inverse division of divcore.cuh on a mu-limb dividend and an
+    mv-limb divisor, both normalised to full length): the Newton steps'
+    low product V*Y mod B^(s+1) and short product Y*|E| (columns >= 2p-1),
+    the quotient's short product u*Y (columns >= P+K-2) and the low product
+    q*v mod B^(K+1)."""
+    def pairs(la, lb, lo, hi):
+        n = 0
+        for c in range(max(lo, 0), hi):
+            i0, i1 = max(0, c - lb + 1), min(la - 1, c)
+            if i1 >= i0:
+                n += i1 - i0 + 1
+        return n
+
+    K, H = mv, mu
+    Qlen = H - K + 1
+    P = Qlen + 1
+    sched, x = [P], P
+    while x > 2:
+        x = (x + 2) // 2
+        sched.append(x)
+    total, p = 0, 1
+    for pn in reversed(sched):
+        if pn <= p:
+            continue
+        sl = pn + 1
+        total += pairs(sl, p + 1, 0, sl + 1)
+        total += pairs(p + 1, sl + 1, (2 * p - 1) // 8 * 8, p + sl + 2)
+        p = pn
+    total += pairs(H, P + 1, (P + K - 2) // 8 * 8, H + P + 1)
+    total += pairs(Qlen + 1, K, 0, K + 1)
+    return total
+
+
 def measure_extra(B, L, stream, args):
     """Multiply and division workloads: instances/s and word-product rates."""
     import torch
@@ -285,7 +320,10 @@ def measure_extra(B, L, stream, args):
         st = torch.empty(n, dtype=torch.uint8, device="cuda")
         ms = event_time(stream, lambda: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
                                                                st.data_ptr(), 2 * mv, mv, n, sp)), 3, 1)
-        div[f"m{mv}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4)}
+        wp = 4 * div_limb_products(2 * mv, mv)   # 32x32-bit word products per division
+        div[f"m{mv}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4),
+                              "word_products_per_div": wp, "word_products_per_s": wp * n / ms * 1e3,
+                              "frac_of_intpipe_peak": round(wp * n / ms * 1e3 / peak_wps, 4)}
         del u, v, q, rr, st
     out["div_u64_2m_by_m"] = div
     out["uneven_batch"] = measure_uneven_batch(B, L, stream)
