@@ -39,7 +39,72 @@ static int launch_mul(const void* a, const void* b, void* r, uint32_t n, cudaStr
     return cudaGetLastError() == cudaSuccess ? 0 : 3;
 }
 
+// The reference's second benchmark type (cuda/main.cu:154-158, 329-337):
+// ten chained additions (baddKer3Bench, and baddKer1Bench whose result is the
+// thesis's 10(u+v) -- baddKer3Bench adds into the buffer it reads, which
+// drops the carries of steps 2..10) and six chained multiplications
+// (convMul5Bench), same geometry as above.
+template <class Base, uint32_t m>
+static int launch_add10(const void* a, const void* b, void* r, uint32_t n, cudaStream_t s) {
+    constexpr uint32_t q = (m / 4 <= 1024) ? 4 : (m + 1024 - 1) / 1024;
+    constexpr uint32_t ipb = (256 + m / q - 1) / (m / q);
+    using uint_t = typename Base::uint_t;
+    if (n % ipb) return 2;
+    baddKer3Bench<Base, m, q, ipb, 10><<<n / ipb, ipb * (m / q), 0, s>>>((uint_t*)a, (uint_t*)b, (uint_t*)r);
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
+
+// baddKer1Bench: one instance per block of m threads (m <= 1024).
+template <class Base, uint32_t m>
+static int launch_add10_v1(const void* a, const void* b, void* r, uint32_t n, cudaStream_t s) {
+    using uint_t = typename Base::uint_t;
+    baddKer1Bench<Base, m, 10><<<n, m, 0, s>>>((uint_t*)a, (uint_t*)b, (uint_t*)r);
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
+
+template <class Base, uint32_t m>
+static int launch_mul6(const void* a, const void* b, void* r, uint32_t n, cudaStream_t s) {
+    constexpr uint32_t q = 4;
+    constexpr uint32_t ipb = (128 + (m / q) - 1) / (m / q);
+    using uint_t = typename Base::uint_t;
+    if (n % ipb) return 2;
+    convMul5Bench<Base, m, ipb, 6><<<n / ipb, ipb * (m / q), 0, s>>>((uint_t*)a, (uint_t*)b, (uint_t*)r);
+    return cudaGetLastError() == cudaSuccess ? 0 : 3;
+}
+
 extern "C" {
+
+int ref_add10_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (m) {
+    case 16: return launch_add10<U64bits, 16>(a, b, r, n, s);
+    case 128: return launch_add10<U64bits, 128>(a, b, r, n, s);
+    case 1024: return launch_add10<U64bits, 1024>(a, b, r, n, s);
+    case 4096: return launch_add10<U64bits, 4096>(a, b, r, n, s);
+    default: return 1;
+    }
+}
+
+int ref_add10v1_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (m) {
+    case 16: return launch_add10_v1<U64bits, 16>(a, b, r, n, s);
+    case 128: return launch_add10_v1<U64bits, 128>(a, b, r, n, s);
+    case 1024: return launch_add10_v1<U64bits, 1024>(a, b, r, n, s);
+    default: return 1;
+    }
+}
+
+int ref_mul6_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (m) {
+    case 64: return launch_mul6<U64bits, 64>(a, b, r, n, s);
+    case 256: return launch_mul6<U64bits, 256>(a, b, r, n, s);
+    case 1024: return launch_mul6<U64bits, 1024>(a, b, r, n, s);
+    default: return 1;
+    }
+}
+
 
 // r = (a + b) mod B^m with the reference's best addition kernel (C-V3).
 int ref_add_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {

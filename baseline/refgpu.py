@@ -41,7 +41,7 @@ def lib():
     global _lib
     if _lib is None and os.path.exists(LIB):
         L = ctypes.CDLL(LIB)
-        for name in ("ref_add_u64", "ref_mul_u64", "ref_mul_u32"):
+        for name in ("ref_add_u64", "ref_mul_u64", "ref_mul_u32", "ref_add10_u64", "ref_add10v1_u64", "ref_mul6_u64"):
             f = getattr(L, name)
             f.argtypes = [ctypes.c_void_p] * 3 + [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
             f.restype = ctypes.c_int
@@ -52,3 +52,6 @@ def lib():
 ADD_SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096]   # u64 limbs
 MUL_SIZES_U64 = [64, 128, 256, 512, 1024, 2048]
 MUL_SIZES_U32 = [64, 128]
+ADD10_SIZES = [16, 128, 1024, 4096]   # u64 limbs (baddKer3Bench<..., 10>)
+ADD10_V1_SIZES = [16, 128, 1024]      # baddKer1Bench<..., 10> (one instance per block, m <= 1024)
+MUL6_SIZES = [64, 256, 1024]          # u64 limbs (convMul5Bench<..., 6>)

@@ -328,6 +328,7 @@ def measure_extra(B, L, stream, args):
     out["div_u64_2m_by_m"] = div
     out["uneven_batch"] = measure_uneven_batch(B, L, stream)
     out["reference_cuda_kernels"] = measure_reference_kernels(B, L, stream)
+    out["chains"] = measure_chains(B, L, stream)
     out["serving"] = measure_serving(B)
     torch.cuda.empty_cache()
     return out
@@ -449,6 +450,66 @@ def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100
             "loop_smem_bytes": info["smem_bytes"],
             "result_arena_limbs": info["arena_limbs"], "per_request_streams": streams,
             "note": "open-loop Poisson replay; latency = completion seen by the host - scheduled arrival"}
+
+
+def measure_chains(B, L, stream):
+    """The reference's second benchmark type: ten chained additions
+    (add chain p = 10, GB/s as 3 n m 8 / time, intermediates on chip) and six
+    chained truncated multiplications (mul chain p = 6), beside the
+    reference's own baddKer3Bench / convMul5Bench on the same inputs."""
+    import torch
+
+    from bigint_gb300.workloads import addsub_u64_device, device_uniform_u64
+
+    sys.path.insert(0, os.path.join(REPO, "baseline"))
+    import refgpu
+
+    R = refgpu.lib() if refgpu.build() else None
+    sp = int(stream.cuda_stream)
+    out = {"add10_u64_gbs": {}, "mul6_u64": {}}
+    for m in refgpu.ADD10_SIZES:
+        a, b = addsub_u64_device(m * 64, seed=SEED_ADDSUB, total_limbs=1 << 27, op="add")
+        n = a.shape[0]
+        r = torch.empty_like(a)
+        ms = event_time(stream, lambda: check(L, L.bi_add_chain_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(),
+                                                                     m, n, 10, sp)), 5)
+        row = {"ours": round(3 * n * m * 8 / ms / 1e6, 1)}
+        if R is not None:
+            rr = torch.empty_like(a)
+            # baddKer3Bench: the reference's fastest ten-addition kernel (same additions; its
+            # in-place buffers drop the carries of steps 2..10, so its values differ)
+            if R.ref_add10_u64(a.data_ptr(), b.data_ptr(), rr.data_ptr(), m, n, sp) == 0:
+                ms_r = event_time(stream, lambda: R.ref_add10_u64(a.data_ptr(), b.data_ptr(), rr.data_ptr(), m, n,
+                                                                  sp), 5)
+                row["reference_baddKer3Bench"] = round(3 * n * m * 8 / ms_r / 1e6, 1)
+            # baddKer1Bench computes 10(a+b): the values to match
+            if m in refgpu.ADD10_V1_SIZES and R.ref_add10v1_u64(a.data_ptr(), b.data_ptr(), rr.data_ptr(), m, n,
+                                                                sp) == 0:
+                ms_1 = event_time(stream, lambda: R.ref_add10v1_u64(a.data_ptr(), b.data_ptr(), rr.data_ptr(), m,
+                                                                    n, sp), 3)
+                row["reference_baddKer1Bench"] = round(3 * n * m * 8 / ms_1 / 1e6, 1)
+                row["bit_exact_vs_baddKer1Bench"] = bool((rr == r).all())
+        out["add10_u64_gbs"][str(m * 64)] = row
+        del a, b, r
+    for m, n in [(64, 1 << 16), (256, 1 << 14), (1024, 1 << 12)]:
+        a = device_uniform_u64(21, n, m)
+        b = device_uniform_u64(22, n, m)
+        r = torch.empty_like(a)
+        ms = event_time(stream, lambda: check(L, L.bi_mul_chain_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(),
+                                                                     m, n, 6, sp)), 5)
+        wp = n * 6 * 4 * m * (m + 1) // 2          # six truncated products, 32x32-bit word products
+        row = {"ours_inst_per_s": round(n / ms * 1e3), "ours_word_products_per_s": wp / ms * 1e3}
+        if R is not None:
+            rr = torch.empty_like(a)
+            if R.ref_mul6_u64(a.data_ptr(), b.data_ptr(), rr.data_ptr(), m, n, sp) == 0:
+                ms_r = event_time(stream, lambda: R.ref_mul6_u64(a.data_ptr(), b.data_ptr(), rr.data_ptr(), m, n,
+                                                                 sp), 5)
+                row["reference_convMul5Bench_inst_per_s"] = round(n / ms_r * 1e3)
+                row["bit_exact"] = bool((rr == r).all())
+        out["mul6_u64"][f"m{m}_n{n}"] = row
+        del a, b, r
+    torch.cuda.empty_cache()
+    return out
 
 
 def measure_reference_kernels(B, L, stream):

@@ -110,6 +110,10 @@ SIGNATURES: dict[str, list] = {
     "bi_batch_noalloc_max_descs": [],
     "bi_batch_run_noalloc": [_P, _U64, _P, _P, _P, _P],
     "bi_probe_intpipe": [_P, _P],
+    "bi_add_chain_u64": [_P, _P, _P, _U32, _U64, _U32, _P],
+    "bi_add_chain_u32": [_P, _P, _P, _U32, _U64, _U32, _P],
+    "bi_mul_chain_u64": [_P, _P, _P, _U32, _U64, _U32, _P],
+    "bi_mul_chain_u32": [_P, _P, _P, _U32, _U64, _U32, _P],
     "bi_server_create": [_P, _P, _U64, _P, _U64, _U32, _U32, _U32, _U32],
     "bi_server_submit": [_P, _P, _P],
     "bi_server_poll": [_P, _P, _U32, _P],
@@ -245,6 +249,28 @@ def div(u, v, q=None, r=None, status=None, stream=None):
     _check(getattr(lib(), f"bi_div_{_wsuffix(u)}")(u.data_ptr(), v.data_ptr(), q.data_ptr(), r.data_ptr(),
                                                   status.data_ptr(), mu, mv, n, _stream_ptr(stream)))
     return q, r, status
+
+
+def add_chain(a, b, p: int, out=None, stream=None):
+    """r1 = a + b, then p-1 times r = r1 + r: p (a + b) mod B^m per row."""
+    _dev2d(a, "a")
+    _dev2d(b, "b")
+    n, m = a.shape
+    r = out if out is not None else a.new_empty(a.shape)
+    _check(getattr(lib(), f"bi_add_chain_{_wsuffix(a)}")(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, p,
+                                                         _stream_ptr(stream)))
+    return r
+
+
+def mul_chain(a, b, p: int, out=None, stream=None):
+    """r1 = a * b, then p-1 times r = r1 * r, truncated: (a b)^p mod B^m per row."""
+    _dev2d(a, "a")
+    _dev2d(b, "b")
+    n, m = a.shape
+    r = out if out is not None else a.new_empty(a.shape)
+    _check(getattr(lib(), f"bi_mul_chain_{_wsuffix(a)}")(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, p,
+                                                         _stream_ptr(stream)))
+    return r
 
 
 def fill_splitmix64(t, seed: int, offset: int = 0, stream=None):

@@ -516,6 +516,96 @@ addsub_chunk_kernel(const T* a, const T* b, T* r, uint8_t* sign_out, uint32_t cp
     }
 }
 
+// ---------------------------------------------------------------------------
+// Fused add chain, the reference's "ten additions" benchmark
+// (baddKer1Bench, cuda/ker-add.cu.h:88-112; the thesis's 10(u+v),
+// thesis/sections/performance.tex:28-36): r1 = a + b, then p-1 times
+// r = r1 + r, i.e. r = p (a + b) mod B^m.  Each step is a full addition with
+// its own carry resolution; r1 and r stay in registers between steps and
+// touch HBM once each way.  Chunked layout as addsub_chunk_kernel.
+// ---------------------------------------------------------------------------
+template <typename T, int W>
+__global__ void __launch_bounds__(W * 32, 1024 / (W * 32))
+addchain_chunk_kernel(const T* a, const T* b, T* r, uint32_t cpi, uint64_t n, uint32_t ipt, uint64_t ntiles,
+                      uint32_t steps) {
+    constexpr int K = 64 / sizeof(T);
+    __shared__ uint32_t s_gp[W];
+    __shared__ uint32_t s_first[W];
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warp = threadIdx.x >> 5;
+    const uint32_t q = threadIdx.x / cpi;
+    const uint32_t pos = threadIdx.x - q * cpi;
+
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t inst0 = tile * (uint64_t)ipt;
+        const uint64_t left = n - inst0;
+        const uint32_t ninst = left < ipt ? (uint32_t)left : ipt;
+        const bool valid = q < ninst;
+        const uint64_t off = (inst0 * cpi + threadIdx.x) * (uint64_t)K;
+        T x[K], y[K];
+        if (valid) {
+            load_chunk<T, K>(a + off, x);
+            load_chunk<T, K>(b + off, y);
+        } else {
+#pragma unroll
+            for (int e = 0; e < K; e++) x[e] = y[e] = 0;
+        }
+        const uint32_t S = __ballot_sync(0xffffffffu, valid && pos == 0);
+        const uint32_t kill = S >> 1;
+        for (uint32_t step = 0; step < steps; step++) {
+            if (step == 1) {   // y = r1 = a + b from now on
+#pragma unroll
+                for (int e = 0; e < K; e++) y[e] = x[e];
+            }
+            uint32_t g, p;
+            {
+                T t[K];
+#pragma unroll
+                for (int e = 0; e < K; e++) t[e] = x[e];
+                g = chunk_chain<OP_ADD, T, K>(t, y, 0u);
+                T acc = (T)~(T)0;
+#pragma unroll
+                for (int e = 0; e < K; e++) acc &= x[e] ^ y[e];
+                p = acc == (T)~(T)0;
+                if (!valid) g = p = 0;
+            }
+            const uint32_t A = __ballot_sync(0xffffffffu, g | p) & ~kill;
+            const uint32_t B = __ballot_sync(0xffffffffu, g) & ~kill;
+            if (lane == 0) {
+                const uint32_t g0 = warp_carry_resolve(A, B, 0).cout;
+                const uint32_t g1 = warp_carry_resolve(A, B, 1).cout;
+                s_gp[warp] = g0 | ((g1 & ~g0) << 1);
+                s_first[warp] = S & 1u;
+            }
+            __syncthreads();
+            const bool before = lane < warp;
+            const bool killed = before && s_first[lane + 1 < W ? lane + 1 : 0];
+            const uint32_t gp = before ? s_gp[lane] : 0u;
+            const bool live = before && !killed;
+            const uint32_t A2 = __ballot_sync(0xffffffffu, live && (gp & 3u));
+            const uint32_t B2 = __ballot_sync(0xffffffffu, live && (gp & 1u));
+            uint32_t cin = (warp_carry_resolve(A2, B2, 0).carries >> warp) & 1u;
+            if (S & 1u) cin = 0;
+            const uint32_t cl = (warp_carry_resolve(A, B, cin).carries >> lane) & 1u;
+            if (valid) chunk_chain<OP_ADD, T, K>(x, y, cl);
+            __syncthreads();   // s_gp is rewritten by the next step
+        }
+        if (valid) store_chunk<T, K>(r + off, x);
+    }
+}
+
+template <typename T, int W>
+static bi_status launch_addchain_cfg(const T* a, const T* b, T* r, uint32_t m, uint64_t n, uint32_t steps,
+                                     cudaStream_t st) {
+    constexpr uint32_t K = 64 / sizeof(T);
+    const uint32_t cpi = m / K;
+    const uint32_t ipt = (W * 32) / cpi;
+    const uint64_t ntiles = (n + ipt - 1) / ipt;
+    const unsigned grid = (unsigned)(ntiles < (1ull << 30) ? ntiles : (1ull << 30));
+    addchain_chunk_kernel<T, W><<<grid, W * 32, 0, st>>>(a, b, r, cpi, n, ipt, ntiles, steps);
+    return check_launch("add chain kernel");
+}
+
 template <typename T, int W, int OP>
 static bi_status launch_chunk_cfg(const T* a, const T* b, T* r, uint8_t* sign, uint32_t m, uint64_t n,
                                   cudaStream_t st) {
@@ -603,6 +693,35 @@ static bi_status addsub(const T* a, const T* b, T* r, uint8_t* sign, uint32_t m,
     return launch_vec<T, 1, OP>(a, b, r, sign, m, n, st);
 }
 
+// r = p (a + b) mod B^m by p chained additions (see addchain_chunk_kernel);
+// sizes the chunked kernel cannot take run as p separate launches into r
+// (which then must not alias a or b).
+template <typename T>
+static bi_status add_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n, uint32_t steps, bi_stream s) {
+    if (n == 0) return BI_OK;
+    if (steps == 0) return set_error(BI_EINVAL, "add chain: p must be >= 1");
+    if (m == 0) return set_error(BI_EINVAL, "m must be >= 1");
+    if (!a || !b || !r) return set_error(BI_EINVAL, "NULL buffer");
+    if ((uintptr_t)a % sizeof(T) || (uintptr_t)b % sizeof(T) || (uintptr_t)r % sizeof(T))
+        return set_error(BI_EINVAL, "buffers must be aligned to the limb size");
+    if ((uint64_t)n * m > (1ull << 46)) return set_error(BI_EINVAL, "n*m too large");
+    constexpr uint32_t KC = 64 / sizeof(T);
+    cudaStream_t st = (cudaStream_t)s;
+    if (((uintptr_t)a | (uintptr_t)b | (uintptr_t)r) % 32 == 0 && m % KC == 0 && m <= 32 * 32 * KC) {
+        if (m <= 8 * 32 * KC) return launch_addchain_cfg<T, 8>(a, b, r, m, n, steps, st);
+        if (m <= 16 * 32 * KC) return launch_addchain_cfg<T, 16>(a, b, r, m, n, steps, st);
+        return launch_addchain_cfg<T, 32>(a, b, r, m, n, steps, st);
+    }
+    if (steps > 1 && (r == a || r == b)) return set_error(BI_EINVAL, "add chain: r must not alias a or b at this size");
+    BI_RETURN_IF((addsub<T, OP_ADD>(a, b, r, nullptr, m, n, s)));   // r1
+    for (uint32_t k = 1; k < steps; k++) {
+        // r = r1 + r with r1 = a + b recomputed on the fly: r += a, then r += b
+        BI_RETURN_IF((addsub<T, OP_ADD>(r, a, r, nullptr, m, n, s)));
+        BI_RETURN_IF((addsub<T, OP_ADD>(r, b, r, nullptr, m, n, s)));
+    }
+    return BI_OK;
+}
+
 bi_status add_link_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n, bi_stream s) {
     return addsub<uint64_t, OP_ADD>(a, b, r, nullptr, m, n, s, true);
 }
@@ -642,6 +761,14 @@ bi_status bi_sub_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint8_t*
 bi_status bi_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint8_t* sign, uint32_t m,
                      uint64_t n, bi_stream s) {
     return addsub<uint32_t, OP_SUB>(a, b, r, sign, m, n, s);
+}
+bi_status bi_add_chain_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n, uint32_t p,
+                           bi_stream s) {
+    return add_chain<uint64_t>(a, b, r, m, n, p, s);
+}
+bi_status bi_add_chain_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n, uint32_t p,
+                           bi_stream s) {
+    return add_chain<uint32_t>(a, b, r, m, n, p, s);
 }
 
 }  // extern "C"

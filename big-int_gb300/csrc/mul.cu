@@ -66,6 +66,68 @@ mul_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, 
     mul_cta<C>(g, smem, scratch, lpdiv, load, store);
 }
 
+// Fused multiply chain, the reference's "six multiplications" benchmark
+// kernel (convMul5Bench, cuda/ker-mul.cu.h:668-695): r1 = a*b, then p-1
+// times r = r1*r, every product truncated to m limbs -- (a*b)^p mod B^m.
+// The first product and the running one stay in shared memory (`first`,
+// `cur`, after the multiply's own area); only a, b and the final r touch HBM.
+template <typename T>
+__global__ void __launch_bounds__(512)
+mulchain_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, uint64_t n, MulGeom g,
+                FastDiv lpdiv, uint32_t steps) {
+    extern __shared__ __align__(16) uint64_t smem[];
+    uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + (size_t)g.ipc * g.IS);
+    uint64_t* first = smem + (size_t)g.ipc * g.IS + 48;   // after 96 words of scratch
+    uint64_t* cur = first + (size_t)g.ipc * g.L;
+    const uint64_t inst0 = (uint64_t)blockIdx.x * g.ipc;
+    // an odd u32 m: the u64 view's top limb keeps only its low word (mod B^m)
+    const uint64_t topmask = (sizeof(T) == 4 && (g.m & 1)) ? 0xffffffffull : ~0ull;
+    // step 0 reads a, b from global memory and fills first and cur; later
+    // steps read first and cur and rewrite cur (one inlined multiply)
+    for (uint32_t k = 0; k < steps; k++) {
+        auto load = [&](uint32_t li, uint32_t x, uint64_t& va, uint64_t& vb) {
+            if (k > 0) {
+                va = first[(size_t)li * g.L + x];
+                vb = cur[(size_t)li * g.L + x];
+                return;
+            }
+            const uint64_t gi = inst0 + li;
+            if (gi >= n) return;
+            if constexpr (sizeof(T) == 8) {
+                va = a[gi * g.m + x];
+                vb = b[gi * g.m + x];
+            } else {
+                const uint64_t w0 = gi * g.m + 2 * x;
+                va = a[w0];
+                vb = b[w0];
+                if (2 * x + 1 < g.m) {
+                    va |= (uint64_t)a[w0 + 1] << 32;
+                    vb |= (uint64_t)b[w0 + 1] << 32;
+                }
+            }
+        };
+        auto store = [&](uint32_t li, uint32_t x, uint64_t v) {
+            if (x == g.L - 1) v &= topmask;
+            if (k == 0) first[(size_t)li * g.L + x] = v;
+            cur[(size_t)li * g.L + x] = v;
+        };
+        mul_cta<MUL_C>(g, smem, scratch, lpdiv, load, store);
+    }
+    // the final value to global memory
+    for (uint32_t idx = threadIdx.x; idx < g.ipc * g.L; idx += blockDim.x) {
+        const uint32_t li = idx / g.L, x = idx - li * g.L;
+        const uint64_t gi = inst0 + li;
+        if (gi >= n) continue;
+        const uint64_t v = cur[idx];
+        if constexpr (sizeof(T) == 8) {
+            r[gi * g.m + x] = v;
+        } else {
+            r[gi * g.m + 2 * x] = (uint32_t)v;
+            if (2 * x + 1 < g.m) r[gi * g.m + 2 * x + 1] = (uint32_t)(v >> 32);
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 
 constexpr uint32_t MUL_MAX_L = 4096;   // u64-view limbs per operand
@@ -102,11 +164,46 @@ static bi_status mul_entry(const T* a, const T* b, T* r, uint32_t m, uint64_t n,
     return mul_launch<T, FULL>(a, b, r, m, n, (cudaStream_t)s);
 }
 
+template <typename T>
+static bi_status mul_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n, uint32_t steps, bi_stream s) {
+    if (n == 0) return BI_OK;
+    if (steps == 0) return set_error(BI_EINVAL, "mul chain: p must be >= 1");
+    if (m == 0) return set_error(BI_EINVAL, "m must be >= 1");
+    if (!a || !b || !r) return set_error(BI_EINVAL, "NULL buffer");
+    if ((uintptr_t)a % sizeof(T) || (uintptr_t)b % sizeof(T) || (uintptr_t)r % sizeof(T))
+        return set_error(BI_EINVAL, "buffers must be aligned to the limb size");
+    const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
+    if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul chain: m=%u above the supported size", m);
+    const uint64_t fill = (n + 2ull * num_sms() - 1) / (2ull * num_sms());
+    MulGeom g = mul_geometry(L, false, fill < 256 ? (uint32_t)(fill ? fill : 1) : 256u);
+    g.m = m;
+    g.out_words = m;
+    const uint32_t threads = (g.ipc * g.tpi + 31) / 32 * 32;
+    const size_t smem = (size_t)g.ipc * g.IS * 8 + 3 * 32 * 4 + 2 * (size_t)g.ipc * g.L * 8;
+    if (smem > 227 * 1024) return set_error(BI_EUNSUPPORTED, "mul chain: m=%u needs too much shared memory", m);
+    auto kern = mulchain_kernel<T>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return set_error(BI_ECUDA, "mul chain: %s", cudaGetErrorString(e));
+    const uint64_t blocks = (n + g.ipc - 1) / g.ipc;
+    if (blocks > 0x7fffffffull) return set_error(BI_EINVAL, "mul chain: n too large");
+    kern<<<(unsigned)blocks, threads, smem, (cudaStream_t)s>>>(a, b, r, n, g, FastDiv(g.Lp), steps);
+    return check_launch("mul chain kernel");
+}
+
 }  // namespace bi
 
 using namespace bi;
 
 extern "C" {
+
+bi_status bi_mul_chain_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n, uint32_t p,
+                           bi_stream s) {
+    return mul_chain<uint64_t>(a, b, r, m, n, p, s);
+}
+bi_status bi_mul_chain_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n, uint32_t p,
+                           bi_stream s) {
+    return mul_chain<uint32_t>(a, b, r, m, n, p, s);
+}
 
 uint32_t bi_max_limbs_mul_u64(void) { return MUL_MAX_L; }
 uint32_t bi_max_limbs_mul_u32(void) { return 2 * MUL_MAX_L; }

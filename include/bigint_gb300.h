@@ -158,6 +158,27 @@ bi_status bi_host_sub_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
                           uint8_t* sign, uint32_t m, uint64_t n);
 
 /* ---------------------------------------------------------------------- */
+/* Fused chains: the reference's second benchmark type, consecutive       */
+/* operations in one kernel with intermediates kept on chip               */
+/* (thesis/sections/performance.tex:28-36).  p >= 1.                       */
+/*  - add chain = baddKer1Bench<..., p> (cuda/ker-add.cu.h:88-112), the    */
+/*    thesis's 10(u+v): r1 = a + b, then p-1 times r = r1 + r, i.e.        */
+/*    r = p (a + b) mod B^m; sizes that are not a multiple of 64 bytes     */
+/*    (or unaligned buffers) run as separate launches, r not aliasing a/b; */
+/*  - mul chain = convMul*Bench<..., p> (cuda/ker-mul.cu.h:223-250,        */
+/*    668-695): r1 = a b, then p-1 times r = r1 r, all truncated to m      */
+/*    limbs, i.e. r = (a b)^p mod B^m.                                     */
+/* ---------------------------------------------------------------------- */
+bi_status bi_add_chain_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                           uint32_t m, uint64_t n, uint32_t p, bi_stream stream);
+bi_status bi_add_chain_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                           uint32_t m, uint64_t n, uint32_t p, bi_stream stream);
+bi_status bi_mul_chain_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
+                           uint32_t m, uint64_t n, uint32_t p, bi_stream stream);
+bi_status bi_mul_chain_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
+                           uint32_t m, uint64_t n, uint32_t p, bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
 /* Uneven batches: instances of different operations and sizes in one      */
 /* graph-captured launch.  The reference launches one template-specialised */
 /* kernel per (operation, size) (cuda/main.cu:476-515); a plan instead     */

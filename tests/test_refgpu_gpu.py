@@ -90,3 +90,57 @@ def test_mul2048_u32_matches_reference_kernel(bigint, ref):
     assert ref.lib().ref_mul_u32(da.data_ptr(), db.data_ptr(), rf.data_ptr(), 2 * m, n, _sp()) == 0
     ours = B.mulfull(B.to_device(a), B.to_device(b))
     assert bool((ours == rf).all())
+
+
+@pytest.mark.parametrize("m", [16, 128, 1024])
+def test_add_chain_matches_reference_ten_additions(bigint, ref, m):
+    """bi_add_chain with p = 10 against baddKer1Bench<U64bits, m, 10>, whose
+    result is the thesis's 10(u+v)."""
+    import torch
+
+    B = bigint
+    n = max(256, 65536 // m)
+    a = uniform_limbs(920 + m, n, m)
+    b = uniform_limbs(921 + m, n, m)
+    a[0] = np.iinfo(np.uint64).max
+    b[0] = 0
+    b[0, 0] = 1
+    da, db = B.to_device(a), B.to_device(b)
+    rr = torch.empty_like(da)
+    assert ref.lib().ref_add10v1_u64(da.data_ptr(), db.data_ptr(), rr.data_ptr(), m, n, _sp()) == 0
+    assert bool((B.add_chain(da, db, 10) == rr).all())
+
+
+def test_reference_v3_ten_additions_drops_carries(bigint, ref, oracle):
+    """baddKer3Bench adds into the buffer it reads (ker-add.cu.h:283-291), so
+    from the second step on it compares each new limb with itself and loses
+    every carry: steps 2..10 double each limb on its own.  Documented here
+    on an input whose first sum has a limb with its top bit set."""
+    import torch
+
+    B = bigint
+    m, n = 16, 256
+    a = uniform_limbs(940, n, m)
+    b = uniform_limbs(941, n, m)
+    da, db = B.to_device(a), B.to_device(b)
+    rr = torch.empty_like(da)
+    assert ref.lib().ref_add10_u64(da.data_ptr(), db.data_ptr(), rr.data_ptr(), m, n, _sp()) == 0
+    got = B.to_host(rr, np.uint64)
+    r1 = oracle.add(a, b)
+    limbwise = (r1 << np.uint64(9))            # each limb doubled nine times, no carries
+    assert (got == limbwise).all()
+    assert not (got == B.to_host(B.add_chain(da, db, 10), np.uint64)).all()
+
+
+@pytest.mark.parametrize("m", [64, 256, 1024])
+def test_mul_chain_matches_reference_six_multiplications(bigint, ref, m):
+    """bi_mul_chain with p = 6 against convMul5Bench<U64bits, m, ipb, 6>."""
+    import torch
+
+    B = bigint
+    n = 256
+    da = B.to_device(uniform_limbs(930 + m, n, m))
+    db = B.to_device(uniform_limbs(931 + m, n, m))
+    rr = torch.empty_like(da)
+    assert ref.lib().ref_mul6_u64(da.data_ptr(), db.data_ptr(), rr.data_ptr(), m, n, _sp()) == 0
+    assert bool((B.mul_chain(da, db, 6) == rr).all())
