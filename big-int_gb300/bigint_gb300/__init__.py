@@ -114,6 +114,26 @@ SIGNATURES: dict[str, list] = {
     "bi_add_chain_u32": [_P, _P, _P, _U32, _U64, _U32, _P],
     "bi_mul_chain_u64": [_P, _P, _P, _U32, _U64, _U32, _P],
     "bi_mul_chain_u32": [_P, _P, _P, _U32, _U64, _U32, _P],
+    "bi_cmp_u64": [_P, _P, _P, _U32, _U64, _P],
+    "bi_cmp_u32": [_P, _P, _P, _U32, _U64, _P],
+    "bi_findk_u64": [_P, _P, _P, _U32, _U64, _P],
+    "bi_findk_u32": [_P, _P, _P, _U32, _U64, _P],
+    "bi_shift_u64": [_P, _P, ctypes.c_int32, _U32, _U64, _P],
+    "bi_shift_u32": [_P, _P, ctypes.c_int32, _U32, _U64, _P],
+    "bi_muld_u64": [_P, _P, _P, _U32, _U64, _P],
+    "bi_muld_u32": [_P, _P, _P, _U32, _U64, _P],
+    "bi_quod_u64": [_P, _P, _P, _P, _U32, _U64, _P],
+    "bi_quod_u32": [_P, _P, _P, _P, _U32, _U64, _P],
+    "bi_test_add_u64": [_P, _P, _P, _U32],
+    "bi_test_add_u32": [_P, _P, _P, _U32],
+    "bi_test_sub_u64": [_P, _P, _P, _U32],
+    "bi_test_sub_u32": [_P, _P, _P, _U32],
+    "bi_test_mul_u64": [_P, _P, _P, _U32],
+    "bi_test_mul_u32": [_P, _P, _P, _U32],
+    "bi_test_div_u64": [_P, _P, _P, _U32],
+    "bi_test_div_u32": [_P, _P, _P, _U32],
+    "bi_limbs_from_words": [_P, ctypes.c_size_t, ctypes.c_size_t, _P, _U32],
+    "bi_limbs_to_words": [_P, _U32, ctypes.c_size_t, _P, _P],
     "bi_server_create": [_P, _P, _U64, _P, _U64, _U32, _U32, _U32, _U32],
     "bi_server_submit": [_P, _P, _P],
     "bi_server_poll": [_P, _P, _U32, _P],
@@ -271,6 +291,87 @@ def mul_chain(a, b, p: int, out=None, stream=None):
     _check(getattr(lib(), f"bi_mul_chain_{_wsuffix(a)}")(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, p,
                                                          _stream_ptr(stream)))
     return r
+
+
+# ---------------------------------------------------------------------------
+# the division prototype's helper primitives, batched (bi_cmp, bi_findk, ...)
+# ---------------------------------------------------------------------------
+
+def cmp(a, b, stream=None):
+    """int8 per row: -1, 0, 1 as a <, ==, > b."""
+    import torch
+
+    _dev2d(a, "a")
+    _dev2d(b, "b")
+    n, m = a.shape
+    out = torch.empty(n, dtype=torch.int8, device=a.device)
+    _check(getattr(lib(), f"bi_cmp_{_wsuffix(a)}")(a.data_ptr(), b.data_ptr(), out.data_ptr(), m, n,
+                                                   _stream_ptr(stream)))
+    return out
+
+
+def findk(a, stream=None):
+    """(k, zero): index of each row's top nonzero limb (0 for zero), and a == 0."""
+    import torch
+
+    _dev2d(a, "a")
+    n, m = a.shape
+    k = torch.empty(n, dtype=torch.int32, device=a.device)
+    z = torch.empty(n, dtype=torch.uint8, device=a.device)
+    _check(getattr(lib(), f"bi_findk_{_wsuffix(a)}")(a.data_ptr(), k.data_ptr(), z.data_ptr(), m, n,
+                                                     _stream_ptr(stream)))
+    return k, z
+
+
+def shift(a, digits: int, stream=None):
+    """Shift each row by whole limbs: up (multiply by B^digits) for digits >= 0."""
+    _dev2d(a, "a")
+    n, m = a.shape
+    r = a.new_empty(a.shape)
+    _check(getattr(lib(), f"bi_shift_{_wsuffix(a)}")(a.data_ptr(), r.data_ptr(), digits, m, n,
+                                                     _stream_ptr(stream)))
+    return r
+
+
+def muld(a, d, stream=None):
+    """r = a * d mod B^m per row, d one limb per row (a tensor of n limbs)."""
+    _dev2d(a, "a")
+    n, m = a.shape
+    r = a.new_empty(a.shape)
+    _check(getattr(lib(), f"bi_muld_{_wsuffix(a)}")(a.data_ptr(), d.data_ptr(), r.data_ptr(), m, n,
+                                                    _stream_ptr(stream)))
+    return r
+
+
+def quod(a, d, stream=None):
+    """(q, rem): floor(a / d) and a mod d per row, d one limb per row."""
+    _dev2d(a, "a")
+    n, m = a.shape
+    q = a.new_empty(a.shape)
+    rem = d.new_empty(d.shape)
+    _check(getattr(lib(), f"bi_quod_{_wsuffix(a)}")(a.data_ptr(), d.data_ptr(), q.data_ptr(), rem.data_ptr(), m, n,
+                                                    _stream_ptr(stream)))
+    return q, rem
+
+
+def limbs_from_words(words: np.ndarray, m: int) -> np.ndarray:
+    """m u64 limbs from a word array in GMP's order -1 (mpz_export(..., -1, size, 0, 0, ...))."""
+    words = np.ascontiguousarray(words)
+    out = np.zeros(m, dtype=np.uint64)
+    _check(lib().bi_limbs_from_words(words.ctypes.data_as(ctypes.c_void_p), words.size, words.itemsize,
+                                     out.ctypes.data_as(ctypes.c_void_p), m))
+    return out
+
+
+def limbs_to_words(limbs: np.ndarray, dtype=np.uint32) -> np.ndarray:
+    """Words of `dtype` in GMP's order -1 without leading zeros (what mpz_export writes)."""
+    limbs = np.ascontiguousarray(limbs, dtype=np.uint64)
+    size = np.dtype(dtype).itemsize
+    out = np.zeros(limbs.size * 8 // size, dtype=dtype)
+    cnt = ctypes.c_size_t()
+    _check(lib().bi_limbs_to_words(limbs.ctypes.data_as(ctypes.c_void_p), limbs.size, size,
+                                   out.ctypes.data_as(ctypes.c_void_p), ctypes.byref(cnt)))
+    return out[: cnt.value]
 
 
 def fill_splitmix64(t, seed: int, offset: int = 0, stream=None):

@@ -223,6 +223,40 @@ static bi_status host_div(const T* hu, const T* hv, T* hq, T* hr, uint8_t* hstat
 
 using namespace bi;
 
+namespace bi {
+
+template <typename T>
+static bi_status test_div(const T* u, const T* v, T* w, uint32_t m,
+                          bi_status (*host_div)(const T*, const T*, T*, T*, uint8_t*, uint32_t, uint32_t, uint64_t)) {
+    if (m == 0) return set_error(BI_EINVAL, "m must be >= 1");
+    if (!u || !v || !w) return set_error(BI_EINVAL, "NULL host buffer");
+    T* rem = (T*)malloc((size_t)m * sizeof(T));
+    if (!rem) return set_error(BI_ENOMEM, "test_div: remainder buffer");
+    const bi_status st = host_div(u, v, w, rem, nullptr, m, m, 1);
+    free(rem);
+    return st;
+}
+static uint64_t read_word(const unsigned char* p, size_t size) {
+    switch (size) {
+        case 1: return *p;
+        case 2: { uint16_t x; memcpy(&x, p, 2); return x; }
+        case 4: { uint32_t x; memcpy(&x, p, 4); return x; }
+        default: { uint64_t x; memcpy(&x, p, 8); return x; }
+    }
+}
+static void write_word(unsigned char* p, size_t size, uint64_t v) {
+    switch (size) {
+        case 1: *p = (unsigned char)v; break;
+        case 2: { const uint16_t x = (uint16_t)v; memcpy(p, &x, 2); break; }
+        case 4: { const uint32_t x = (uint32_t)v; memcpy(p, &x, 4); break; }
+        default: memcpy(p, &v, 8);
+    }
+}
+
+}  // namespace bi
+
+using namespace bi;
+
 extern "C" {
 
 bi_status bi_host_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r, uint8_t* status,
@@ -249,6 +283,69 @@ const char* bi_status_string(bi_status s) {
 }
 
 const char* bi_last_error(void) { return g_err; }
+
+// ---- the Futhark library's 1-D entries: one instance through the host twins
+bi_status bi_test_add_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m) {
+    return bi_host_add_u64(u, v, w, m, 1);
+}
+bi_status bi_test_add_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m) {
+    return bi_host_add_u32(u, v, w, m, 1);
+}
+bi_status bi_test_sub_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m) {
+    uint8_t sign;
+    return bi_host_sub_u64(u, v, w, &sign, m, 1);
+}
+bi_status bi_test_sub_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m) {
+    uint8_t sign;
+    return bi_host_sub_u32(u, v, w, &sign, m, 1);
+}
+bi_status bi_test_mul_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m) {
+    return bi_host_mul_u64(u, v, w, m, 1);
+}
+bi_status bi_test_mul_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m) {
+    return bi_host_mul_u32(u, v, w, m, 1);
+}
+bi_status bi_test_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m) {
+    return test_div<uint64_t>(u, v, w, m, bi_host_div_u64);
+}
+bi_status bi_test_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m) {
+    return test_div<uint32_t>(u, v, w, m, bi_host_div_u32);
+}
+
+// ---- GMP word arrays (order -1, native byte order) <-> 64-bit limbs
+bi_status bi_limbs_from_words(const void* words, size_t count, size_t size, uint64_t* limbs, uint32_t m) {
+    if (!(size == 1 || size == 2 || size == 4 || size == 8)) return set_error(BI_EINVAL, "word size must be 1, 2, 4 or 8");
+    if (!limbs || (count && !words)) return set_error(BI_EINVAL, "NULL buffer");
+    const size_t per = 8 / size;   // words per limb
+    const unsigned char* w = (const unsigned char*)words;
+    for (uint32_t j = 0; j < m; j++) limbs[j] = 0;
+    for (size_t k = 0; k < count; k++) {
+        const uint64_t x = read_word(w + k * size, size);
+        const size_t j = k / per;
+        if (j >= m) {
+            if (x != 0) return set_error(BI_EINVAL, "value needs more than m=%u limbs", m);
+            continue;
+        }
+        limbs[j] |= x << (8 * size * (k % per));
+    }
+    return BI_OK;
+}
+
+bi_status bi_limbs_to_words(const uint64_t* limbs, uint32_t m, size_t size, void* words, size_t* count) {
+    if (!(size == 1 || size == 2 || size == 4 || size == 8)) return set_error(BI_EINVAL, "word size must be 1, 2, 4 or 8");
+    if (!limbs || !words || !count) return set_error(BI_EINVAL, "NULL buffer");
+    const size_t per = 8 / size;
+    const uint64_t mask = size == 8 ? ~0ull : ((1ull << (8 * size)) - 1);
+    unsigned char* w = (unsigned char*)words;
+    size_t used = 0;
+    for (size_t k = 0; k < (size_t)m * per; k++) {
+        const uint64_t x = (limbs[k / per] >> (8 * size * (k % per))) & mask;
+        write_word(w + k * size, size, x);
+        if (x) used = k + 1;
+    }
+    *count = used;
+    return BI_OK;
+}
 
 int bi_version(void) { return 100; }
 

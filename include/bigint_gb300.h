@@ -179,6 +179,74 @@ bi_status bi_mul_chain_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
                            uint32_t m, uint64_t n, uint32_t p, bi_stream stream);
 
 /* ---------------------------------------------------------------------- */
+/* The division prototype's helper primitives as batched device ops       */
+/* (prototypes/div.c:49-202; Futhark forms futhark/helper.fut:83-124,     */
+/* futhark/div.fut:21-69), over [n][m] limbs:                              */
+/*  bi_cmp:   out[i] = -1, 0, 1 as a_i <, ==, > b_i (lt, eq, :49-62);      */
+/*  bi_findk: k[i] = index of a_i's top nonzero limb, 0 for zero (findk,   */
+/*            :92-96; prec = k + 1), zero[i] = (a_i == 0) (ez, :64-69);    */
+/*            either output may be NULL;                                   */
+/*  bi_shift: shift by whole limbs (shift, :104-117): digits >= 0 gives    */
+/*            r_i = a_i * B^digits mod B^m, digits < 0 r_i = a_i / B^-digits;*/
+/*            r must not alias a;                                          */
+/*  bi_muld:  r_i = a_i * d_i mod B^m with one limb d_i (multd, :197-217);  */
+/*  bi_quod:  q_i = floor(a_i / d_i), rem_i = a_i mod d_i (rem may be NULL)*/
+/*            with one limb d_i (quod, :165-181); d_i = 0 gives 0 and 0;   */
+/*            q must not alias a.                                          */
+/* ---------------------------------------------------------------------- */
+bi_status bi_cmp_u64(const uint64_t* a, const uint64_t* b, int8_t* out,
+                     uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_cmp_u32(const uint32_t* a, const uint32_t* b, int8_t* out,
+                     uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_findk_u64(const uint64_t* a, uint32_t* k, uint8_t* zero,
+                       uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_findk_u32(const uint32_t* a, uint32_t* k, uint8_t* zero,
+                       uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_shift_u64(const uint64_t* a, uint64_t* r, int32_t digits,
+                       uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_shift_u32(const uint32_t* a, uint32_t* r, int32_t digits,
+                       uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_muld_u64(const uint64_t* a, const uint64_t* d, uint64_t* r,
+                      uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_muld_u32(const uint32_t* a, const uint32_t* d, uint32_t* r,
+                      uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_quod_u64(const uint64_t* a, const uint64_t* d, uint64_t* q,
+                      uint64_t* rem, uint32_t m, uint64_t n, bi_stream stream);
+bi_status bi_quod_u32(const uint32_t* a, const uint32_t* d, uint32_t* q,
+                      uint32_t* rem, uint32_t m, uint64_t n, bi_stream stream);
+
+/* ---------------------------------------------------------------------- */
+/* The Futhark library's shape-agnostic entries on one integer of m limbs */
+/* (futhark/test/gmp-validation-lib.fut:13-27), host pointers:            */
+/* test_add = (u + v) mod B^m, test_sub = |u - v|, test_mul = (u v) mod   */
+/* B^m, test_div = floor(u / v) (v = 0: BI_EDIV0 and w = 0).              */
+/* ---------------------------------------------------------------------- */
+bi_status bi_test_add_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m);
+bi_status bi_test_add_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m);
+bi_status bi_test_sub_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m);
+bi_status bi_test_sub_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m);
+bi_status bi_test_mul_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m);
+bi_status bi_test_mul_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m);
+bi_status bi_test_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* w, uint32_t m);
+bi_status bi_test_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* w, uint32_t m);
+
+/* ---------------------------------------------------------------------- */
+/* GMP word arrays.  The reference moves integers in and out of GMP with  */
+/* mpz_import / mpz_export in order -1 (least significant word first),    */
+/* native byte order (cuda/helpers.h:161-187, gmp-validation.c:30-52).    */
+/* bi_limbs_from_words reads `count` words of `size` bytes (1, 2, 4 or 8) */
+/* in that order into m 64-bit limbs (zero-extended; BI_EINVAL if the     */
+/* value needs more than m limbs); bi_limbs_to_words writes the value of  */
+/* m limbs as words of `size` bytes, least significant first, without    */
+/* leading zero words (*count = words written, 0 for zero), as mpz_export */
+/* does; `words` must hold ceil(m * 8 / size) words.  Host only.          */
+/* ---------------------------------------------------------------------- */
+bi_status bi_limbs_from_words(const void* words, size_t count, size_t size,
+                              uint64_t* limbs, uint32_t m);
+bi_status bi_limbs_to_words(const uint64_t* limbs, uint32_t m, size_t size,
+                            void* words, size_t* count);
+
+/* ---------------------------------------------------------------------- */
 /* Uneven batches: instances of different operations and sizes in one      */
 /* graph-captured launch.  The reference launches one template-specialised */
 /* kernel per (operation, size) (cuda/main.cu:476-515); a plan instead     */

@@ -180,3 +180,72 @@ def from_int(x: int, m: int, dtype=np.uint64) -> np.ndarray:
     nbytes = m * np.dtype(dtype).itemsize
     x &= (1 << (8 * nbytes)) - 1
     return np.frombuffer(x.to_bytes(nbytes, "little"), dtype=np.dtype(dtype).newbyteorder("<")).astype(dtype)
+
+
+# ---- the division prototype's helper primitives (pure Python, small cases) --
+# Restated from prototypes/div.c on digit arrays of either width; rows of a
+# [n][m] batch are processed one by one.
+
+def cmp_rows(a, b) -> np.ndarray:
+    """-1, 0, 1 per row as a <, ==, > b: lt and eq (div.c:49-62)."""
+    out = np.zeros(a.shape[0], np.int8)
+    for i in range(a.shape[0]):
+        res = 0
+        for j in range(a.shape[1]):          # lt's loop: the last difference decides
+            if a[i, j] != b[i, j]:
+                res = -1 if a[i, j] < b[i, j] else 1
+        out[i] = res
+    return out
+
+
+def findk_rows(a):
+    """(k, zero) per row: findk (div.c:92-96) and ez (div.c:64-69)."""
+    k = np.zeros(a.shape[0], np.int64)
+    z = np.zeros(a.shape[0], np.uint8)
+    for i in range(a.shape[0]):
+        kk = 0
+        for j in range(a.shape[1]):
+            kk = j if a[i, j] != 0 else kk
+        k[i] = kk
+        z[i] = 1 if not a[i].any() else 0
+    return k, z
+
+
+def shift_rows(a, n: int):
+    """shift (div.c:104-117): n >= 0 moves digits up, n < 0 down."""
+    m = a.shape[1]
+    r = np.zeros_like(a)
+    for j in range(m):
+        src = j - n
+        if 0 <= src < m:
+            r[:, j] = a[:, src]
+    return r
+
+
+def muld_rows(a, d):
+    """multd (div.c:197-217): a * d mod B^m with one digit d per row."""
+    m = a.shape[1]
+    out = np.zeros_like(a)
+    for i in range(a.shape[0]):
+        out[i] = from_int(to_int(a[i]) * int(d[i]), m, a.dtype)
+    return out
+
+
+def quod_rows(a, d):
+    """quod (div.c:165-181): long division by one digit d per row; also the
+    remainder.  d = 0 gives 0 and 0."""
+    m = a.shape[1]
+    bits = a.dtype.itemsize * 8
+    q = np.zeros_like(a)
+    rem = np.zeros(a.shape[0], a.dtype)
+    for i in range(a.shape[0]):
+        dd = int(d[i])
+        if dd == 0:
+            continue
+        r = 0
+        for j in range(m - 1, -1, -1):       # top digit first, as div.c
+            r = (r << bits) + int(a[i, j])
+            q[i, j] = r // dd
+            r -= (r // dd) * dd
+        rem[i] = r
+    return q, rem

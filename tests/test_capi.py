@@ -90,3 +90,27 @@ def test_server_rejects_bad_arguments_on_host(L):
     assert L.bi_server_poll(None, None, 0, None) == 1
     assert L.bi_server_destroy(None) == 0
     assert L.bi_status_string(7) == b"BI_EBUSY"
+
+
+def test_gmp_word_converters_round_trip(L):
+    """bi_limbs_from_words / bi_limbs_to_words against Python integers: GMP's
+    order -1 word arrays of 1, 2, 4 and 8 bytes (host code, no GPU)."""
+    import numpy as np
+
+    import bigint_gb300 as B
+
+    rng = np.random.default_rng(5)
+    for dt in (np.uint8, np.uint16, np.uint32, np.uint64):
+        for nbits in (0, 1, 63, 64, 65, 1000, 4096):
+            x = int(rng.integers(0, 2**62)) ** 80 % (1 << nbits) if nbits else 0
+            size = np.dtype(dt).itemsize
+            nw = max(1, (nbits + 8 * size - 1) // (8 * size))
+            words = np.array([(x >> (8 * size * k)) & ((1 << (8 * size)) - 1) for k in range(nw)], dtype=dt)
+            m = max(1, (nbits + 63) // 64)
+            limbs = B.limbs_from_words(words, m)
+            assert sum(int(v) << (64 * j) for j, v in enumerate(limbs)) == x
+            back = B.limbs_to_words(limbs, dt)
+            assert sum(int(v) << (8 * size * k) for k, v in enumerate(back)) == x
+            assert len(back) == 0 if x == 0 else back[-1] != 0        # no leading zero words
+    with pytest.raises(B.BigIntError):
+        B.limbs_from_words(np.array([1, 2, 3], dtype=np.uint64), 2)   # needs 3 limbs

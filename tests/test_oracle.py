@@ -150,3 +150,35 @@ def test_exact_oracle_division_random(oracle):
         for i in range(n):
             U, V = _int(u[i]), _int(v[i])
             assert _int(q[i]) == U // V and _int(r[i]) == U % V
+
+
+def test_primitive_restatements_against_python_ints(oracle):
+    """The oracle's restatements of div.c's helpers against Python integers."""
+    from bigint_gb300.workloads import uniform_limbs
+
+    O = oracle
+    for dtype, bits in ((np.uint64, 64), (np.uint32, 32)):
+        a = uniform_limbs(71, 40, 9, dtype)
+        b = a.copy()
+        b[::3, 4] ^= dtype(1)
+        a[5] = 0
+        a[6, 3:] = 0
+        ints_a = [O.to_int(r) for r in a]
+        ints_b = [O.to_int(r) for r in b]
+        assert list(O.cmp_rows(a, b)) == [(x > y) - (x < y) for x, y in zip(ints_a, ints_b)]
+        k, z = O.findk_rows(a)
+        assert list(z) == [1 if x == 0 else 0 for x in ints_a]
+        assert list(k) == [max(0, (x.bit_length() - 1) // bits) for x in ints_a]
+        for sh in (-3, 0, 2, 9):
+            r = O.shift_rows(a, sh)
+            want = [(x << (bits * sh)) % (1 << (bits * 9)) if sh >= 0 else x >> (bits * -sh) for x in ints_a]
+            assert [O.to_int(row) for row in r] == want
+        d = uniform_limbs(72, 40, 1, dtype)[:, 0]
+        d[0] = 0
+        d[1] = 1
+        d[2] = np.iinfo(dtype).max
+        assert [O.to_int(r) for r in O.muld_rows(a, d)] == [(x * int(dd)) % (1 << (bits * 9)) for x, dd in zip(ints_a, d)]
+        q, rem = O.quod_rows(a, d)
+        for x, dd, qq, rr in zip(ints_a, d, q, rem):
+            dd = int(dd)
+            assert O.to_int(qq) == (x // dd if dd else 0) and int(rr) == (x % dd if dd else 0)
