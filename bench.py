@@ -181,6 +181,33 @@ def event_time(stream, fn, reps: int, warmup: int = 2):
     return e0.elapsed_time(e1) / reps
 
 
+def graph_time(fn_on, reps: int = 20):
+    """ms per call of fn_on(stream_handle) from one replay of a CUDA graph of
+    `reps` captured calls: for launches short enough that the host's per-call
+    overhead would otherwise set the interval."""
+    import torch
+
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        for _ in range(2):
+            fn_on(int(s.cuda_stream))
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s):
+        for _ in range(reps):
+            fn_on(int(s.cuda_stream))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(s):             # replay() launches on the current stream
+        g.replay()
+        torch.cuda.synchronize()
+        e0.record(s)
+        g.replay()
+        e1.record(s)
+    torch.cuda.synchronize()
+    del g
+    return e0.elapsed_time(e1) / reps
+
+
 def check(L, st):
     if st != 0:
         raise RuntimeError(f"library call failed: {L.bi_last_error().decode()}")
@@ -307,9 +334,26 @@ def measure_extra(B, L, stream, args):
     a, b = mul2048_u32()
     da, db = B.to_device(a), B.to_device(b)
     r = torch.empty((a.shape[0], 128), dtype=torch.int32, device="cuda")
-    ms = event_time(stream, lambda: check(L, L.bi_mulfull_u32(da.data_ptr(), db.data_ptr(), r.data_ptr(), 64, 4096, sp)), 20)
+    ms = graph_time(lambda st: check(L, L.bi_mulfull_u32(da.data_ptr(), db.data_ptr(), r.data_ptr(), 64, 4096, st)))
+    ms_ev = event_time(stream, lambda: check(L, L.bi_mulfull_u32(da.data_ptr(), db.data_ptr(), r.data_ptr(), 64, 4096, sp)), 20)
     out["mul2048_u32"] = {"instances_per_s": round(4096 / ms * 1e3), "ms": round(ms, 5),
-                          "note": "4096 pairs of 64 u32 limbs, 10% all-ones, full 128-limb product"}
+                          "instances_per_s_python_launches": round(4096 / ms_ev * 1e3),
+                          "note": "4096 pairs of 64 u32 limbs, 10% all-ones, full 128-limb product; a launch this "
+                                  "short is timed as one replay of a CUDA graph of 20 launches (host overhead "
+                                  "excluded, as for the reference kernel beside it)"}
+    # small full products (the warp-level path): 2^27 limbs of input per size, graph-timed
+    small = {}
+    for m in (2, 4, 8, 16, 32):
+        n = (1 << 22) // m
+        a = device_uniform_u64(31, n, m)
+        b = device_uniform_u64(32, n, m)
+        r = torch.empty((n, 2 * m), dtype=torch.int64, device="cuda")
+        ms = graph_time(lambda st: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, st)), 5)
+        wp = n * (2 * m) ** 2
+        small[f"m{m}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "word_products_per_s": wp / ms * 1e3,
+                               "frac_of_intpipe_peak": round(wp / ms * 1e3 / peak_wps, 4)}
+        del a, b, r
+    out["mulfull_u64_small"] = small
     div = {}
     for mv, n in [(4, 1 << 16), (16, 1 << 14), (64, 1 << 13), (256, 1 << 12), (1024, 1 << 10)]:
         u = device_uniform_u64(11, n, 2 * mv)
@@ -570,7 +614,7 @@ def measure_reference_kernels(B, L, stream):
     pb[:, :m] = b
     dpa, dpb = B.to_device(pa), B.to_device(pb)
     rf = torch.empty_like(dpa)
-    ms_ref = event_time(stream, lambda: R.ref_mul_u32(dpa.data_ptr(), dpb.data_ptr(), rf.data_ptr(), 2 * m, n, sp), 20)
+    ms_ref = graph_time(lambda st: R.ref_mul_u32(dpa.data_ptr(), dpb.data_ptr(), rf.data_ptr(), 2 * m, n, st))
     res["mul2048_u32_full_reference_inst_per_s"] = round(n / ms_ref * 1e3)
     return res
 

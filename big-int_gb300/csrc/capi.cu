@@ -9,6 +9,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
+#include <mutex>
+#include <vector>
+
 #include "common.cuh"
 
 namespace bi {
@@ -29,11 +33,43 @@ bi_status check_launch(const char* what) {
     return BI_OK;
 }
 
+// SM count of the current device, queried once per device.
 int num_sms() {
+    static std::atomic<int> cache[64];
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+    if (dev >= 0 && dev < 64 && (sms = cache[dev].load(std::memory_order_relaxed)) != 0) return sms;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 148;
+    if (dev >= 0 && dev < 64) cache[dev].store(sms, std::memory_order_relaxed);
     return sms;
+}
+
+// Raise a kernel's dynamic shared-memory limit to `smem` on the current
+// device; remembered per (kernel, device), so a launch path calls the driver
+// only the first time it needs a larger size.
+cudaError_t smem_opt_in(const void* func, size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    struct Entry {
+        const void* func;
+        int dev;
+        size_t smem;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(mu);
+    for (Entry& x : done)
+        if (x.func == func && x.dev == dev) {
+            if (x.smem >= smem) return cudaSuccess;
+            e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e == cudaSuccess) x.smem = smem;
+            return e;
+        }
+    e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) done.push_back({func, dev, smem});
+    return e;
 }
 
 static bi_status cuda_ok(cudaError_t e, const char* what) {

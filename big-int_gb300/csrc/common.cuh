@@ -122,6 +122,7 @@ namespace bi {
 bi_status set_error(bi_status st, const char* fmt, ...);
 bi_status check_launch(const char* what);
 int num_sms();
+cudaError_t smem_opt_in(const void* func, size_t smem);
 // add/sub on pinned host buffers read over the CPU-GPU link (addsub.cu)
 bi_status add_link_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n, bi_stream s);
 bi_status add_link_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n, bi_stream s);

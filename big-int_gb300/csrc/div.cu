@@ -87,7 +87,7 @@ static bi_status div_entry(const T* u, const T* v, T* q, T* r, uint8_t* status, 
     if (smem > 227 * 1024) return set_error(BI_EUNSUPPORTED, "div: sizes need too much shared memory");
     const int threads = div_threads(g.MU);
     auto kern = div_kernel<T>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = smem_opt_in((const void*)kern, smem);
     if (e != cudaSuccess) return set_error(BI_ECUDA, "div: %s", cudaGetErrorString(e));
     const uint64_t grid = n < (1ull << 30) ? n : (1ull << 30);
     kern<<<(unsigned)grid, threads, smem, (cudaStream_t)s>>>(u, v, q, r, status, n, g);

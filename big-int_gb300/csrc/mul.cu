@@ -129,14 +129,170 @@ mulchain_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict_
 }
 
 // ---------------------------------------------------------------------------
+// Warp-level full product for small operands: G lanes per instance (G = the
+// power of two >= L, several instances per warp when L < 32; written for
+// P = Lpad / G column pairs per lane, which also covers L up to 128 with
+// G = 32), no CTA barrier.  The library routes full products of
+// L <= MUL_WARP_MAX_L = 32 here: faster than the CTA kernel at L = 32
+// (2048 bits), slower at L = 64, where each lane's column loop costs more
+// instructions per word product than the CTA kernel's row windows.  Operands padded to Lpad = G*P limbs sit in the
+// warp's shared memory; lane t of an instance accumulates the product
+// columns t + G*j, j < 2P, as 3-word sums (mul.lo/hi + add.cc chain),
+// pairing low column j with high column 2P-1-j so every lane does
+// G(2j+1) terms in phase j.  The column sums s_c = c0 + c1 B + c2 B^2 are
+// folded into limbs by two additions row by row (c0 + c1 shifted one column,
+// then + c2 shifted two), carries resolved with ballots within the instance.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mac3(uint64_t& c0, uint64_t& c1, uint64_t& c2, uint64_t x, uint64_t y) {
+    asm("{\n\t.reg .u64 lo, hi;\n\t"
+        "mul.lo.u64 lo, %3, %4;\n\tmul.hi.u64 hi, %3, %4;\n\t"
+        "add.cc.u64 %0, %0, lo;\n\taddc.cc.u64 %1, %1, hi;\n\taddc.u64 %2, %2, 0;\n\t}"
+        : "+l"(c0), "+l"(c1), "+l"(c2)
+        : "l"(x), "l"(y));
+}
+
+// carry into lane t of a G-lane group (lanes base..base+G-1) for per-lane
+// (generate, propagate) and carry-in cin; cout = carry out of the group
+__device__ __forceinline__ uint32_t group_carry(uint32_t g, uint32_t p, uint32_t cin, uint32_t G, uint32_t base,
+                                                uint32_t t, uint32_t& cout) {
+    const uint32_t Aw = __ballot_sync(0xffffffffu, g | p), Bw = __ballot_sync(0xffffffffu, g);
+    const uint64_t gm = G == 32 ? 0xffffffffull : ((1ull << G) - 1);
+    const uint64_t A = (Aw >> base) & gm, B = (Bw >> base) & gm;
+    const uint64_t s = A + B + cin;
+    cout = (uint32_t)(s >> G) & 1u;
+    return (uint32_t)((s ^ A ^ B) >> t) & 1u;
+}
+
+template <typename T, int P, int G>
+__global__ void __launch_bounds__(256)
+mul_warp_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, uint64_t n, uint32_t m,
+                uint32_t L) {
+    extern __shared__ __align__(16) uint64_t smem[];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t Lpad = G * P;
+    const uint32_t ipw = 32 / G;                       // instances per warp
+    const uint32_t lg = lane / G, t = lane - lg * G;   // instance within the warp, lane within it
+    const uint32_t base = lg * G;
+    uint64_t* sa = smem + ((size_t)warp * ipw + lg) * 2 * Lpad;
+    uint64_t* sb = sa + Lpad;
+    const uint32_t out_limbs = 2 * L;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t wi = (uint64_t)blockIdx.x * (blockDim.x >> 5) + warp; wi * ipw < n; wi += nwarps) {
+        const uint64_t inst = wi * ipw + lg;
+        const bool valid = inst < n;
+        for (uint32_t x = t; x < Lpad; x += G) {
+            uint64_t va = 0, vb = 0;
+            if (valid && x < L) {
+                if constexpr (sizeof(T) == 8) {
+                    va = a[inst * m + x];
+                    vb = b[inst * m + x];
+                } else {
+                    const uint64_t w0 = inst * m + 2 * x;
+                    va = a[w0];
+                    vb = b[w0];
+                    if (2 * x + 1 < m) {
+                        va |= (uint64_t)a[w0 + 1] << 32;
+                        vb |= (uint64_t)b[w0 + 1] << 32;
+                    }
+                }
+            }
+            sa[x] = va;
+            sb[x] = vb;
+        }
+        __syncwarp();
+        uint64_t acc[2 * P][3];
+#pragma unroll
+        for (int j = 0; j < P; j++) {
+            const uint32_t lo = t + G * j;                  // a low column ...
+            const uint32_t hi = t + G * (2 * P - 1 - j);    // ... and its high partner (>= Lpad)
+            const uint32_t hi_i0 = hi - Lpad + 1;           // first row of the high column
+            const uint32_t len = G * (2 * j + 1);           // terms of both, the same in every lane
+            uint64_t c0 = 0, c1 = 0, c2 = 0;
+#pragma unroll
+            for (uint32_t rr = 0; rr < len; rr++) {
+                const bool low = rr <= lo;
+                const uint32_t i = low ? rr : hi_i0 + (rr - lo - 1);
+                const uint32_t col = low ? lo : hi;
+                mac3(c0, c1, c2, sa[i], sb[col - i]);
+                if (rr == lo) {
+                    acc[j][0] = c0; acc[j][1] = c1; acc[j][2] = c2;
+                    c0 = c1 = c2 = 0;
+                }
+            }
+            acc[2 * P - 1 - j][0] = c0; acc[2 * P - 1 - j][1] = c1; acc[2 * P - 1 - j][2] = c2;
+        }
+        __syncwarp();   // the shared operands are rewritten by the next round
+        // fold: row jj holds columns G*jj + t
+        uint32_t cy1 = 0, cy2 = 0;                  // carries between rows (both additions)
+        uint64_t prev1 = 0, prev2a = 0, prev2b = 0;  // c1 of column G*jj-1; c2 of columns G*jj-2, G*jj-1
+#pragma unroll
+        for (int jj = 0; jj < 2 * P; jj++) {
+            // c1 of column c-1 and c2 of column c-2
+            uint64_t s1 = __shfl_up_sync(0xffffffffu, acc[jj][1], 1, G);
+            if (t == 0) s1 = prev1;
+            uint64_t s2 = __shfl_up_sync(0xffffffffu, acc[jj][2], 2, G);
+            if (t == 0) s2 = prev2a;
+            else if (t == 1) s2 = prev2b;
+            prev1 = __shfl_sync(0xffffffffu, acc[jj][1], base + G - 1);
+            prev2a = __shfl_sync(0xffffffffu, acc[jj][2], base + G - 2);
+            prev2b = __shfl_sync(0xffffffffu, acc[jj][2], base + G - 1);
+            // y = c0 + s1
+            const uint64_t y = acc[jj][0] + s1;
+            uint32_t co;
+            const uint32_t k1 = group_carry(y < s1, y == ~0ull, cy1, G, base, t, co);
+            cy1 = co;
+            const uint64_t y2 = y + k1;
+            // v = y2 + s2
+            const uint64_t v = y2 + s2;
+            const uint32_t k2 = group_carry(v < s2, v == ~0ull, cy2, G, base, t, co);
+            cy2 = co;
+            const uint32_t c = G * jj + t;
+            if (valid && c < out_limbs) {
+                const uint64_t out = v + k2;
+                if constexpr (sizeof(T) == 8) {
+                    r[inst * out_limbs + c] = out;
+                } else {
+                    const uint64_t w0 = inst * (2ull * m) + 2 * c;
+                    if (2 * c < 2 * m) r[w0] = (uint32_t)out;
+                    if (2 * c + 1 < 2 * m) r[w0 + 1] = (uint32_t)(out >> 32);
+                }
+            }
+        }
+    }
+}
+
+template <typename T, int P, int G>
+static bi_status mul_warp_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, uint32_t L, cudaStream_t st) {
+    constexpr uint32_t ipw = 32 / G;
+    const uint64_t warps = (n + ipw - 1) / ipw;
+    const uint64_t blocks = (warps + 7) / 8;
+    const uint64_t cap = (uint64_t)num_sms() * 32;
+    const size_t smem = (size_t)8 * ipw * 2 * G * P * 8;
+    mul_warp_kernel<T, P, G><<<(unsigned)(blocks < cap ? blocks : cap), 256, smem, st>>>(a, b, r, n, m, L);
+    return check_launch("mulfull warp kernel");
+}
+
+// Full products of u64-view size L <= MUL_WARP_MAX_L go to the warp kernel.
+template <typename T>
+static bi_status mul_warp(const T* a, const T* b, T* r, uint32_t m, uint64_t n, uint32_t L, cudaStream_t st) {
+    if (L <= 2) return mul_warp_launch<T, 1, 2>(a, b, r, m, n, L, st);
+    if (L <= 4) return mul_warp_launch<T, 1, 4>(a, b, r, m, n, L, st);
+    if (L <= 8) return mul_warp_launch<T, 1, 8>(a, b, r, m, n, L, st);
+    if (L <= 16) return mul_warp_launch<T, 1, 16>(a, b, r, m, n, L, st);
+    return mul_warp_launch<T, 1, 32>(a, b, r, m, n, L, st);
+}
+
+// ---------------------------------------------------------------------------
 
 constexpr uint32_t MUL_MAX_L = 4096;   // u64-view limbs per operand
+constexpr uint32_t MUL_WARP_MAX_L = 32;    // full products up to here take the warp kernel
 
 template <typename T, bool FULL>
 static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     constexpr int C = MUL_C;
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
+    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, L, st);
     // at least two CTAs per SM when the batch is small: fewer instances per CTA
     const uint64_t fill = (n + 2ull * num_sms() - 1) / (2ull * num_sms());
     MulGeom g = mul_geometry(L, FULL, fill < 256 ? (uint32_t)(fill ? fill : 1) : 256u);
@@ -146,7 +302,7 @@ static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n
     const size_t smem = (size_t)g.ipc * g.IS * 8 + 3 * 32 * 4;
     if (smem > 227 * 1024) return set_error(BI_EUNSUPPORTED, "mul: m=%u needs too much shared memory", m);
     auto kern = mul_kernel<T, C, FULL>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = smem_opt_in((const void*)kern, smem);
     if (e != cudaSuccess) return set_error(BI_ECUDA, "mul: %s", cudaGetErrorString(e));
     const uint64_t blocks = (n + g.ipc - 1) / g.ipc;
     if (blocks > 0x7fffffffull) return set_error(BI_EINVAL, "mul: n too large");
@@ -182,7 +338,7 @@ static bi_status mul_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n,
     const size_t smem = (size_t)g.ipc * g.IS * 8 + 3 * 32 * 4 + 2 * (size_t)g.ipc * g.L * 8;
     if (smem > 227 * 1024) return set_error(BI_EUNSUPPORTED, "mul chain: m=%u needs too much shared memory", m);
     auto kern = mulchain_kernel<T>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = smem_opt_in((const void*)kern, smem);
     if (e != cudaSuccess) return set_error(BI_ECUDA, "mul chain: %s", cudaGetErrorString(e));
     const uint64_t blocks = (n + g.ipc - 1) / g.ipc;
     if (blocks > 0x7fffffffull) return set_error(BI_EINVAL, "mul chain: n too large");
