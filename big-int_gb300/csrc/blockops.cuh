@@ -1,8 +1,8 @@
 // blockops.cuh -- CTA-cooperative big-integer primitives on shared memory.
 //
-// Every function here is called by all threads of the CTA with the same
-// arguments (block-uniform control flow) and contains __syncthreads.  Limbs
-// are 64-bit, little-endian.  These are the batched-division building blocks:
+// Every function here is called by all threads of a cooperating group -- the
+// whole CTA (CtaGroup, the default) or one warp (WarpGroup) -- with the same
+// arguments, and synchronises that group.  Limbs are 64-bit, little-endian.  These are the batched-division building blocks:
 // the reference's division prototype composes the same primitives (shift,
 // compare, findk, add, sub, mult; prototypes/div.c:49-218, and their parallel
 // forms in futhark/helper.fut:101-124 and futhark/div.fut:21-69).
@@ -58,34 +58,83 @@ __device__ __forceinline__ uint32_t block_max_u32(uint32_t v, uint32_t* scratch)
     return x;
 }
 
+// The threads that cooperate on one number.  CtaGroup: the whole CTA, with
+// __syncthreads and shared-memory exchanges through `scratch`.  WarpGroup: the
+// calling warp alone (other warps may be doing anything), with __syncwarp,
+// ballots and shuffles -- no CTA barrier.
+struct CtaGroup {
+    static __device__ __forceinline__ int rank() { return (int)threadIdx.x; }
+    static __device__ __forceinline__ int size() { return (int)blockDim.x; }
+    static __device__ __forceinline__ void sync() { __syncthreads(); }
+    static __device__ __forceinline__ uint32_t carry_in(uint32_t g, uint32_t p, bool seg, uint32_t* scratch) {
+        return block_carry_in(g, p, seg, scratch);
+    }
+    static __device__ __forceinline__ uint32_t max_u32(uint32_t v, uint32_t* scratch) {
+        return block_max_u32(v, scratch);
+    }
+    // v as held by rank src
+    static __device__ __forceinline__ uint32_t bcast(uint32_t v, int src, uint32_t* scratch) {
+        if ((int)threadIdx.x == src) scratch[100] = v;
+        __syncthreads();
+        const uint32_t r = scratch[100];
+        __syncthreads();
+        return r;
+    }
+};
+
+struct WarpGroup {
+    static __device__ __forceinline__ int rank() { return (int)(threadIdx.x & 31); }
+    static __device__ __forceinline__ int size() { return 32; }
+    static __device__ __forceinline__ void sync() { __syncwarp(); }
+    static __device__ __forceinline__ uint32_t carry_in(uint32_t g, uint32_t p, bool seg, uint32_t*) {
+        const uint32_t kill = __ballot_sync(0xffffffffu, seg) >> 1;
+        const uint32_t A = __ballot_sync(0xffffffffu, g | p) & ~kill;
+        const uint32_t B = __ballot_sync(0xffffffffu, g) & ~kill;
+        return (warp_carry_resolve(A, B, 0).carries >> (threadIdx.x & 31)) & 1u;
+    }
+    static __device__ __forceinline__ uint32_t max_u32(uint32_t v, uint32_t*) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+        return v;
+    }
+    static __device__ __forceinline__ uint32_t bcast(uint32_t v, int src, uint32_t*) {
+        return __shfl_sync(0xffffffffu, v, src);
+    }
+};
+
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ void chunk_of(int len, int& lo, int& hi) {
-    const int T = blockDim.x;
+    const int T = Grp::size();
     const int cw = (len + T - 1) / T;
-    lo = threadIdx.x * cw;
+    lo = Grp::rank() * cw;
     hi = lo + cw < len ? lo + cw : len;
     if (lo > len) lo = len;
 }
 
 // number of limbs up to and including the top nonzero one (0 for zero) -- findk + 1
 // (prototypes/div.c:92-101; futhark/div.fut:38-39)
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ int block_prec(const uint64_t* X, int len, uint32_t* scratch) {
     uint32_t best = 0;
-    for (int i = threadIdx.x; i < len; i += blockDim.x)
+    for (int i = Grp::rank(); i < len; i += Grp::size())
         if (X[i] != 0) best = max(best, (uint32_t)(i + 1));
-    return (int)block_max_u32(best, scratch);
+    return (int)Grp::max_u32(best, scratch);
 }
 
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ void block_zero(uint64_t* X, int len) {
-    for (int i = threadIdx.x; i < len; i += blockDim.x) X[i] = 0;
+    for (int i = Grp::rank(); i < len; i += Grp::size()) X[i] = 0;
 }
 
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ void block_copy(uint64_t* dst, const uint64_t* src, int len) {
-    for (int i = threadIdx.x; i < len; i += blockDim.x) dst[i] = src[i];
+    for (int i = Grp::rank(); i < len; i += Grp::size()) dst[i] = src[i];
 }
 
 // out[0..len) = (X << s bits) over len limbs of X (zero above lx); s in [0, 64).  out != X.
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ void block_shl_bits(uint64_t* out, const uint64_t* X, int lx, int len, int s) {
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    for (int i = Grp::rank(); i < len; i += Grp::size()) {
         const uint64_t cur = i < lx ? X[i] : 0;
         const uint64_t prev = (i > 0 && i - 1 < lx) ? X[i - 1] : 0;
         out[i] = s ? ((cur << s) | (prev >> (64 - s))) : cur;
@@ -93,8 +142,9 @@ __device__ __forceinline__ void block_shl_bits(uint64_t* out, const uint64_t* X,
 }
 
 // out[0..len) = X >> s bits (X has lx limbs); s in [0, 64).  out != X.
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ void block_shr_bits(uint64_t* out, const uint64_t* X, int lx, int len, int s) {
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    for (int i = Grp::rank(); i < len; i += Grp::size()) {
         const uint64_t cur = i < lx ? X[i] : 0;
         const uint64_t next = i + 1 < lx ? X[i + 1] : 0;
         out[i] = s ? ((cur >> s) | (next << (64 - s))) : cur;
@@ -106,10 +156,11 @@ __device__ __forceinline__ void block_shr_bits(uint64_t* out, const uint64_t* X,
 // The carries are resolved by block_carry_in over per-thread chunks, i.e. the
 // carry-propagation scan of the reference's badd/bsub (ker-add.cu.h:121-149,
 // futhark/sub.fut:14-26) applied to a single instance held by the whole CTA.
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ uint32_t block_addsub(uint64_t* out, const uint64_t* X, int lx, const uint64_t* Y,
                                                  int ly, int len, bool sub, uint32_t* scratch) {
     int lo, hi;
-    chunk_of(len, lo, hi);
+    chunk_of<Grp>(len, lo, hi);
     uint32_t G = 0, P = 1;
     for (int i = lo; i < hi; i++) {
         const uint64_t x = i < lx ? X[i] : 0, y = i < ly ? Y[i] : 0;
@@ -120,7 +171,7 @@ __device__ __forceinline__ uint32_t block_addsub(uint64_t* out, const uint64_t* 
         P = p & P;
     }
     if (lo >= hi) { G = 0; P = 1; }
-    const uint32_t cin = block_carry_in(G, P, threadIdx.x == 0, scratch);
+    const uint32_t cin = Grp::carry_in(G, P, Grp::rank() == 0, scratch);
     uint32_t c = cin;
     for (int i = lo; i < hi; i++) {
         const uint64_t x = i < lx ? X[i] : 0, y = i < ly ? Y[i] : 0;
@@ -131,29 +182,30 @@ __device__ __forceinline__ uint32_t block_addsub(uint64_t* out, const uint64_t* 
         c = g | (p & c);
     }
     // carry out of the whole number: the last nonempty chunk's final carry
-    const int T = blockDim.x;
+    const int T = Grp::size();
     const int cw = (len + T - 1) / T;
     const int last = cw ? (len - 1) / cw : 0;
-    if ((int)threadIdx.x == last) scratch[100] = c;
-    __syncthreads();
-    const uint32_t r = scratch[100];
-    __syncthreads();
-    return r;
+    return Grp::bcast(c, last, scratch);
 }
 
 // -1, 0, 1 as X <, ==, > Y (both zero-extended to len limbs) -- the reference's
 // lt/eq (prototypes/div.c:49-62; futhark/helper.fut:109-115)
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ int block_cmp(const uint64_t* X, int lx, const uint64_t* Y, int ly, int len,
                                         uint32_t* scratch) {
     uint32_t best = 0;
-    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    for (int i = Grp::rank(); i < len; i += Grp::size()) {
         const uint64_t x = i < lx ? X[i] : 0, y = i < ly ? Y[i] : 0;
         if (x != y) best = max(best, ((uint32_t)(i + 1) << 1) | (x > y ? 1u : 0u));
     }
-    const uint32_t m = block_max_u32(best, scratch);
+    const uint32_t m = Grp::max_u32(best, scratch);
     if (m == 0) return 0;
     return (m & 1u) ? 1 : -1;
 }
+
+// Limbs per 8-column window in block_mul's window buffer: the 10-limb window
+// plus one, an odd stride so consecutive windows fall on different banks.
+constexpr int BLOCK_MUL_WS = 11;
 
 // R[0..10) += O[0..10) with the carry chain.
 __device__ __forceinline__ void add10(uint64_t (&R)[10], const uint64_t (&O)[10]) {
@@ -173,7 +225,7 @@ __device__ __forceinline__ void add10(uint64_t (&R)[10], const uint64_t (&O)[10]
 // below are not written, and the value of out above c_lo falls short of the
 // true product's by less than min(la, lb) * B^(c_lo + 1) -- under one unit
 // two limbs above c_lo.  out must not alias A, Bm or wbuf; wbuf holds
-// ceil(olen/8)*10 limbs.
+// ceil(olen/8)*BLOCK_MUL_WS limbs.
 //
 // Column windows of 8 limbs are accumulated with row_mac8 (as in mul.cu).  The
 // rows of each window are cut into S slices (S a power of two up to 32, the
@@ -181,10 +233,12 @@ __device__ __forceinline__ void add10(uint64_t (&R)[10], const uint64_t (&O)[10]
 // S consecutive lanes and summed with warp shuffles, so a product with few
 // windows still occupies the CTA.  The windows are then merged with a carry
 // lookahead across windows.
+template <typename Grp = CtaGroup>
 __device__ __forceinline__ void block_mul(const uint64_t* A, int la, const uint64_t* Bm, int lb, uint64_t* out,
                                           int olen, uint64_t* wbuf, uint32_t* scratch, int c_lo = 0) {
     constexpr int C = 8;
-    const int T = blockDim.x, t = threadIdx.x, lane = t & 31;
+    constexpr int WS = BLOCK_MUL_WS;   // window stride in wbuf: odd, so lanes' 64-bit accesses spread over the banks
+    const int T = Grp::size(), t = Grp::rank(), lane = t & 31;
     const int W = (olen + C - 1) / C;
     const int w0 = c_lo / C < W ? c_lo / C : W;
     const int NW = W - w0;
@@ -245,10 +299,10 @@ __device__ __forceinline__ void block_mul(const uint64_t* A, int la, const uint6
         }
         if (j < NW * S && sl == 0) {
 #pragma unroll
-            for (int e = 0; e < C + 2; e++) wbuf[w * (C + 2) + e] = R[e];
+            for (int e = 0; e < C + 2; e++) wbuf[w * WS + e] = R[e];
         }
     }
-    __syncthreads();
+    Grp::sync();
     // merge: thread takes windows [u_lo, u_hi); D_u = P_u + O_{u-1} (in place in wbuf)
     const int cw = (NW + T - 1) / T;
     int u_lo = w0 + t * cw, u_hi = u_lo + cw;
@@ -259,13 +313,13 @@ __device__ __forceinline__ void block_mul(const uint64_t* A, int la, const uint6
     for (int u = u_lo; u < u_hi; u++) {
         uint64_t o0 = 0, o1 = 0;
         if (u > w0) {
-            o0 = wbuf[(u - 1) * (C + 2) + C];
-            o1 = wbuf[(u - 1) * (C + 2) + C + 1];
+            o0 = wbuf[(u - 1) * WS + C];
+            o1 = wbuf[(u - 1) * WS + C + 1];
         }
         uint32_t c = 0, all = 1;
         for (int e = 0; e < C; e++) {
             const uint64_t add = e == 0 ? o0 : (e == 1 ? o1 : 0);
-            const uint64_t x = wbuf[u * (C + 2) + e];
+            const uint64_t x = wbuf[u * WS + e];
             const uint64_t s = x + add;
             uint32_t k = s < add;
             const uint64_t s2 = s + c;
@@ -280,19 +334,19 @@ __device__ __forceinline__ void block_mul(const uint64_t* A, int la, const uint6
         P = p & P;
     }
     // the D values are recomputed below (the O limbs are never overwritten)
-    const uint32_t cin = block_carry_in(G, P, t == 0, scratch);
+    const uint32_t cin = Grp::carry_in(G, P, t == 0, scratch);
     uint32_t c_win = cin;
     for (int u = u_lo; u < u_hi; u++) {
         uint64_t o0 = 0, o1 = 0;
         if (u > w0) {
-            o0 = wbuf[(u - 1) * (C + 2) + C];
-            o1 = wbuf[(u - 1) * (C + 2) + C + 1];
+            o0 = wbuf[(u - 1) * WS + C];
+            o1 = wbuf[(u - 1) * WS + C + 1];
         }
         uint32_t c = 0;
         uint32_t cc = c_win;
         for (int e = 0; e < C; e++) {
             const uint64_t add = e == 0 ? o0 : (e == 1 ? o1 : 0);
-            const uint64_t x = wbuf[u * (C + 2) + e];
+            const uint64_t x = wbuf[u * WS + e];
             const uint64_t s = x + add;
             uint32_t k = s < add;
             const uint64_t s2 = s + c;
@@ -306,7 +360,7 @@ __device__ __forceinline__ void block_mul(const uint64_t* A, int la, const uint6
         const uint32_t g = (gs >> (u - u_lo)) & 1u, p = (ps >> (u - u_lo)) & 1u;
         c_win = g | (p & c_win);
     }
-    __syncthreads();
+    Grp::sync();
 }
 
 }  // namespace bi

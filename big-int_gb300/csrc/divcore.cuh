@@ -3,6 +3,8 @@
 // for the algorithm and its correspondence with the reference.
 #pragma once
 
+#include <type_traits>
+
 #include "blockops.cuh"
 
 namespace bi {
@@ -36,11 +38,52 @@ __device__ __forceinline__ uint64_t recip_limb(uint64_t d) {
     return q;
 }
 
-// One division on the CTA: u has g.MU 64-bit limbs, v has g.MV; load_u(i)
-// and load_v(i) supply limbs, store_q(i, x) for i < g.MU and store_r(i, x)
-// for i < g.MV receive the results, set_status(code) the status (thread 0).
-// Every thread of the CTA calls it with the same arguments.
-template <typename LoadU, typename LoadV, typename StoreQ, typename StoreR, typename SetStatus>
+// Newton steps up to this precision (limbs) run on warp 0 alone
+// (WarpGroup): their operands are small, and one warp with __syncwarp
+// finishes them sooner than the whole CTA with its barriers.
+constexpr int DIV_WARP_NEWTON_MAX = 64;
+
+// One Newton step of the shifted inverse, from precision p to pn: Y_p (p + 1
+// limbs at Yb + (Pmax - p)) becomes Y_pn (pn + 1 limbs at Yb + (Pmax - pn)).
+template <typename Grp>
+__device__ __forceinline__ void newton_step(const DivGeom& g, const uint64_t* Vn, int K, uint64_t* Yb, uint64_t* X,
+                                            uint32_t* scratch, int p, int pn) {
+    const uint32_t Pmax = g.Pmax;
+    uint64_t* Vs = X + g.oVs;
+    uint64_t* Tb = X + g.oT;
+    uint64_t* Pr = X + g.oProd;
+    uint64_t* Wb = X + g.oW;
+    const int sl = pn + 1;
+    // divisor prefix: the top sl limbs of v (zero-extended below when K < sl)
+    for (int i = Grp::rank(); i < sl; i += Grp::size()) {
+        const int src = K - sl + i;
+        Vs[i] = src >= 0 ? Vn[src] : 0;
+    }
+    Grp::sync();
+    const uint64_t* Yp = Yb + (Pmax - p);
+    // T = Vs * Y_p mod B^(sl+1); E = B^(sl+p) - Vs*Y_p, |E| < B^(sl+1)/2
+    block_mul<Grp>(Vs, sl, Yp, p + 1, Tb, sl + 1, Wb, scratch);
+    const bool e_neg = (Tb[sl] >> 63) == 0;    // T small: E = -T
+    if (!e_neg) block_addsub<Grp>(Tb, nullptr, 0, Tb, sl + 1, sl + 1, true, scratch);   // |E| = -T
+    // D = floor(Y_p * |E| / B^(2p+1)), from a short product (columns >= 2p-1):
+    // at most one unit short, which the next step's residual absorbs
+    block_mul<Grp>(Yp, p + 1, Tb, sl + 1, Pr, p + sl + 2, Wb, scratch, 2 * p - 1);
+    const uint64_t* D = Pr + 2 * p + 1;
+    const int Dlen = sl - p + 1;
+    // Y_pn = Y_p * B^(pn-p) +/- D
+    for (int i = Grp::rank(); i < pn - p; i += Grp::size()) Yb[Pmax - pn + i] = 0;
+    Grp::sync();
+    uint64_t* Ypn = Yb + (Pmax - pn);
+    block_addsub<Grp>(Ypn, Ypn, pn + 1, D, Dlen, pn + 1, e_neg, scratch);
+}
+
+// One division on a cooperating group (the CTA, or one warp): u has g.MU
+// 64-bit limbs, v has g.MV; load_u(i) and load_v(i) supply limbs,
+// store_q(i, x) for i < g.MU and store_r(i, x) for i < g.MV receive the
+// results, set_status(code) the status (rank 0).  Every thread of the group
+// calls it with the same arguments.
+template <typename Grp = CtaGroup, typename LoadU, typename LoadV, typename StoreQ, typename StoreR,
+          typename SetStatus>
 __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU load_u, LoadV load_v,
                                         StoreQ store_q, StoreR store_r, SetStatus set_status) {
     uint64_t* Un = smem + g.oUn;
@@ -49,37 +92,38 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
     uint64_t* X = smem + g.oX;
     uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + g.smem_limbs);
     const uint32_t MU = g.MU, MV = g.MV, Pmax = g.Pmax;
+    const uint32_t rk = (uint32_t)Grp::rank(), sz = (uint32_t)Grp::size();
     // ---- raw operands: u into X[0, MU), v into X[MU, MU+MV)
     uint64_t* Uraw = X;
     uint64_t* Vraw = X + MU;
-    for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) Uraw[i] = load_u(i);
-    for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) Vraw[i] = load_v(i);
-    __syncthreads();
-    const int K = block_prec(Vraw, (int)MV, scratch);
+    for (uint32_t i = rk; i < MU; i += sz) Uraw[i] = load_u(i);
+    for (uint32_t i = rk; i < MV; i += sz) Vraw[i] = load_v(i);
+    Grp::sync();
+    const int K = block_prec<Grp>(Vraw, (int)MV, scratch);
     if (K == 0) {                                  // division by zero
-        for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) store_q(i, 0);
-        for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) store_r(i, 0);
-        if (threadIdx.x == 0) set_status(1);
-        __syncthreads();
+        for (uint32_t i = rk; i < MU; i += sz) store_q(i, 0);
+        for (uint32_t i = rk; i < MV; i += sz) store_r(i, 0);
+        if (rk == 0) set_status(1);
+        Grp::sync();
         return;
     }
     const int s = __clzll((long long)Vraw[K - 1]);
-    block_shl_bits(Vn, Vraw, K, K, s);
-    block_shl_bits(Un, Uraw, (int)MU, (int)MU + 1, s);
-    __syncthreads();
-    const int H = block_prec(Un, (int)MU + 1, scratch);
+    block_shl_bits<Grp>(Vn, Vraw, K, K, s);
+    block_shl_bits<Grp>(Un, Uraw, (int)MU, (int)MU + 1, s);
+    Grp::sync();
+    const int H = block_prec<Grp>(Un, (int)MU + 1, scratch);
     if (H < K) {                                   // u < v: q = 0, r = u
-        for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) store_q(i, 0);
-        for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) store_r(i, Uraw[i]);
-        if (threadIdx.x == 0) set_status(0);
-        __syncthreads();
+        for (uint32_t i = rk; i < MU; i += sz) store_q(i, 0);
+        for (uint32_t i = rk; i < MV; i += sz) store_r(i, Uraw[i]);
+        if (rk == 0) set_status(0);
+        Grp::sync();
         return;
     }
     const int Qlen = H - K + 1;
     const int P = Qlen + 1;
 
     // ---- shifted inverse: Y_p at Yb + (Pmax - p), p + 1 limbs
-    if (threadIdx.x == 0) {
+    if (rk == 0) {
         Yb[Pmax - 1] = recip_limb(Vn[K - 1]);
         Yb[Pmax] = 1;
         Yb[Pmax + 1] = 0;
@@ -94,37 +138,32 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
             sched[ns++] = x;
         }
     }
-    __syncthreads();
+    Grp::sync();
     int p = 1;
-    uint64_t* Vs = X + g.oVs;
-    uint64_t* Tb = X + g.oT;
-    uint64_t* Pr = X + g.oProd;
-    uint64_t* Wb = X + g.oW;
+    if constexpr (std::is_same<Grp, CtaGroup>::value) {
+        // the small steps on warp 0 alone, then one barrier
+        if (threadIdx.x < 32) {
+            int pw = 1;
+            for (int si = ns - 1; si >= 0; si--) {
+                const int pn = sched[si];
+                if (pn <= pw) continue;
+                if (pn > DIV_WARP_NEWTON_MAX) break;
+                newton_step<WarpGroup>(g, Vn, K, Yb, X, scratch, pw, pn);
+                pw = pn;
+            }
+        }
+        __syncthreads();
+        for (int si = ns - 1; si >= 0; si--) {     // where warp 0 stopped
+            const int pn = sched[si];
+            if (pn <= p) continue;
+            if (pn > DIV_WARP_NEWTON_MAX) break;
+            p = pn;
+        }
+    }
     for (int si = ns - 1; si >= 0; si--) {
         const int pn = sched[si];
         if (pn <= p) continue;
-        const int sl = pn + 1;
-        // divisor prefix: the top sl limbs of v (zero-extended below when K < sl)
-        for (int i = threadIdx.x; i < sl; i += blockDim.x) {
-            const int src = K - sl + i;
-            Vs[i] = src >= 0 ? Vn[src] : 0;
-        }
-        __syncthreads();
-        const uint64_t* Yp = Yb + (Pmax - p);
-        // T = Vs * Y_p mod B^(sl+1); E = B^(sl+p) - Vs*Y_p, |E| < B^(sl+1)/2
-        block_mul(Vs, sl, Yp, p + 1, Tb, sl + 1, Wb, scratch);
-        const bool e_neg = (Tb[sl] >> 63) == 0;    // T small: E = -T
-        if (!e_neg) block_addsub(Tb, nullptr, 0, Tb, sl + 1, sl + 1, true, scratch);   // |E| = -T
-        // D = floor(Y_p * |E| / B^(2p+1)), from a short product (columns >= 2p-1):
-        // at most one unit short, which the next step's residual absorbs
-        block_mul(Yp, p + 1, Tb, sl + 1, Pr, p + sl + 2, Wb, scratch, 2 * p - 1);
-        const uint64_t* D = Pr + 2 * p + 1;
-        const int Dlen = sl - p + 1;
-        // Y_pn = Y_p * B^(pn-p) +/- D
-        for (int i = threadIdx.x; i < pn - p; i += blockDim.x) Yb[Pmax - pn + i] = 0;
-        __syncthreads();
-        uint64_t* Ypn = Yb + (Pmax - pn);
-        block_addsub(Ypn, Ypn, pn + 1, D, Dlen, pn + 1, e_neg, scratch);
+        newton_step<Grp>(g, Vn, K, Yb, X, scratch, p, pn);
         p = pn;
     }
     const uint64_t* Y = Yb + (Pmax - P);
@@ -136,42 +175,42 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
     uint64_t* QV = X + g.oQV;
     uint64_t* Rb = X + g.oR;
     uint64_t* W2 = X + g.oW2;
-    block_mul(Un, H, Y, P + 1, Big, H + P + 1, W2, scratch, P + K - 2);
-    for (int i = threadIdx.x; i < Qlen + 1; i += blockDim.x) Qb[i] = i < Qlen ? Big[P + K + i] : 0;
-    __syncthreads();
+    block_mul<Grp>(Un, H, Y, P + 1, Big, H + P + 1, W2, scratch, P + K - 2);
+    for (int i = rk; i < Qlen + 1; i += sz) Qb[i] = i < Qlen ? Big[P + K + i] : 0;
+    Grp::sync();
 
     // ---- remainder r = u - q*v from the low K+1 limbs, then corrections
-    block_mul(Qb, Qlen + 1, Vn, K, QV, K + 1, W2, scratch);
-    block_addsub(Rb, Un, K + 1, QV, K + 1, K + 1, true, scratch);
+    block_mul<Grp>(Qb, Qlen + 1, Vn, K, QV, K + 1, W2, scratch);
+    block_addsub<Grp>(Rb, Un, K + 1, QV, K + 1, K + 1, true, scratch);
     int fixes = 0;
     bool ok = true;
     while ((Rb[K] >> 63) != 0) {                  // r < 0
         if (++fixes > DIV_MAX_CORRECTIONS) { ok = false; break; }
-        block_addsub(Rb, Rb, K + 1, Vn, K, K + 1, false, scratch);
+        block_addsub<Grp>(Rb, Rb, K + 1, Vn, K, K + 1, false, scratch);
         // q -= 1
         uint64_t* onebuf = QV;                     // QV is free now
-        if (threadIdx.x == 0) onebuf[0] = 1;
-        __syncthreads();
-        block_addsub(Qb, Qb, Qlen + 1, onebuf, 1, Qlen + 1, true, scratch);
+        if (rk == 0) onebuf[0] = 1;
+        Grp::sync();
+        block_addsub<Grp>(Qb, Qb, Qlen + 1, onebuf, 1, Qlen + 1, true, scratch);
     }
     fixes = 0;
-    while (ok && block_cmp(Rb, K + 1, Vn, K, K + 1, scratch) >= 0) {   // r >= v
+    while (ok && block_cmp<Grp>(Rb, K + 1, Vn, K, K + 1, scratch) >= 0) {   // r >= v
         if (++fixes > DIV_MAX_CORRECTIONS) { ok = false; break; }
-        block_addsub(Rb, Rb, K + 1, Vn, K, K + 1, true, scratch);
+        block_addsub<Grp>(Rb, Rb, K + 1, Vn, K, K + 1, true, scratch);
         uint64_t* onebuf = QV;
-        if (threadIdx.x == 0) onebuf[0] = 1;
-        __syncthreads();
-        block_addsub(Qb, Qb, Qlen + 1, onebuf, 1, Qlen + 1, false, scratch);
+        if (rk == 0) onebuf[0] = 1;
+        Grp::sync();
+        block_addsub<Grp>(Qb, Qb, Qlen + 1, onebuf, 1, Qlen + 1, false, scratch);
     }
 
     // ---- outputs: q, and r shifted back by s bits
     uint64_t* Rout = QV;
-    block_shr_bits(Rout, Rb, K, K, s);
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < MU; i += blockDim.x) store_q(i, (int)i < Qlen + 1 ? Qb[i] : 0);
-    for (uint32_t i = threadIdx.x; i < MV; i += blockDim.x) store_r(i, (int)i < K ? Rout[i] : 0);
-    if (threadIdx.x == 0) set_status(ok ? 0 : 2);
-    __syncthreads();
+    block_shr_bits<Grp>(Rout, Rb, K, K, s);
+    Grp::sync();
+    for (uint32_t i = rk; i < MU; i += sz) store_q(i, (int)i < Qlen + 1 ? Qb[i] : 0);
+    for (uint32_t i = rk; i < MV; i += sz) store_r(i, (int)i < K ? Rout[i] : 0);
+    if (rk == 0) set_status(ok ? 0 : 2);
+    Grp::sync();
 }
 
 __host__ __device__ inline DivGeom div_geom(uint32_t mu, uint32_t mv, int wbytes) {
@@ -192,7 +231,7 @@ __host__ __device__ inline DivGeom div_geom(uint32_t mu, uint32_t mv, int wbytes
     g.oProd = g.oT + Pm + 4;
     const uint32_t prodlen = 2 * Pm + 8;
     g.oW = g.oProd + prodlen;
-    const uint32_t endN = g.oW + (prodlen + 7) / 8 * 10 + 10;
+    const uint32_t endN = g.oW + (prodlen + 7) / 8 * BLOCK_MUL_WS + BLOCK_MUL_WS;
     // phases Q and R
     const uint32_t biglen = MU + Pm + 4;
     g.oBig = 0;
@@ -200,7 +239,7 @@ __host__ __device__ inline DivGeom div_geom(uint32_t mu, uint32_t mv, int wbytes
     g.oQV = g.oQ + Pm + 4;
     g.oR = g.oQV + (MV + 4 > Pm + 4 ? MV + 4 : Pm + 4);
     g.oW2 = g.oR + MV + 4;
-    const uint32_t endQ = g.oW2 + (biglen + 7) / 8 * 10 + 10;
+    const uint32_t endQ = g.oW2 + (biglen + 7) / 8 * BLOCK_MUL_WS + BLOCK_MUL_WS;
     // the raw operands are staged in X too
     uint32_t endX = endN > endQ ? endN : endQ;
     if (endX < MU + MV) endX = MU + MV;
