@@ -14,10 +14,12 @@
 //     bucket item (as many instances as fit one CTA, mulcore.cuh);
 //   * divisions go one per CTA to persistent kernels (divcore.cuh), one per
 //     size class of dividend -- under 64 limbs on 64-thread CTAs, under 256
-//     on 128-thread CTAs, the rest on 256-thread CTAs -- each sized for the
-//     shared memory of its own largest division, so small divisions run many
-//     CTAs per SM instead of one; most expensive first within a class.
-// The five persistent kernels run concurrently on forked streams; the fork,
+//     on 128-thread CTAs, under 1024 on 256-thread CTAs, the rest on
+//     512-thread CTAs -- each sized for the shared memory of its own largest
+//     division, so small divisions run many CTAs per SM instead of one and
+//     the largest get as many warps as an SM's registers allow; most
+//     expensive first within a class.
+// The six persistent kernels run concurrently on forked streams; the fork,
 // the launches, the counter reset and the join are captured once into a CUDA
 // graph and replayed by every bi_plan_execute.  Work is handed out with one
 // atomic counter per kernel (no waiting on other CTAs).
@@ -121,12 +123,12 @@ batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
     }
 }
 
-// division size classes by dividend limbs: < 64, < 256, the rest
-constexpr int DIV_CLASSES = 3;
-constexpr int DIV_CLASS_THREADS[DIV_CLASSES] = {64, 128, 256};
+// division size classes by dividend limbs: < 64, < 256, < 1024, the rest
+constexpr int DIV_CLASSES = 4;
+constexpr int DIV_CLASS_THREADS[DIV_CLASSES] = {64, 128, 256, 512};
 constexpr int PLAN_KERNELS = 2 + DIV_CLASSES;   // add/sub, multiply, one per division class
 
-static inline int div_class(uint32_t mu) { return mu < 64 ? 0 : mu < 256 ? 1 : 2; }
+static inline int div_class(uint32_t mu) { return mu < 64 ? 0 : mu < 256 ? 1 : mu < 1024 ? 2 : 3; }
 
 // At most 128 registers a thread, so 512 / THREADS CTAs fit an SM's register file.
 template <int THREADS>
@@ -280,10 +282,11 @@ static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
     if (p->n_divc[0]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[0]>(p->n_divc[0], L->smem[2], sms, &L->grid[2]));
     if (p->n_divc[1]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[1]>(p->n_divc[1], L->smem[3], sms, &L->grid[3]));
     if (p->n_divc[2]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[2]>(p->n_divc[2], L->smem[4], sms, &L->grid[4]));
+    if (p->n_divc[3]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[3]>(p->n_divc[3], L->smem[5], sms, &L->grid[5]));
     return BI_OK;
 }
 
-// s[k] is the stream of kernel k (add/sub, multiply, division classes 0..2).
+// s[k] is the stream of kernel k (add/sub, multiply, division classes 0..3).
 static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags,
                                      const BatchTune& t, const Launch3& L, const cudaStream_t* s,
                                      int comps = COMP_ALL) {
@@ -307,6 +310,11 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
     }
     if (comps & COMP_DIV) {
         // the largest class first: its divisions take longest
+        if (p->n_divc[3]) {
+            batch_div_kernel<DIV_CLASS_THREADS[3]><<<L.grid[5], DIV_CLASS_THREADS[3], L.smem[5], s[5]>>>(
+                p->d_descs, p->d_div + p->div_off[3], p->n_divc[3], p->d_counters + 5, in, out, flags);
+            BI_RETURN_IF(check_launch("batch div kernel"));
+        }
         if (p->n_divc[2]) {
             batch_div_kernel<DIV_CLASS_THREADS[2]><<<L.grid[4], DIV_CLASS_THREADS[2], L.smem[4], s[4]>>>(
                 p->d_descs, p->d_div + p->div_off[2], p->n_divc[2], p->d_counters + 4, in, out, flags);
@@ -530,7 +538,8 @@ static float time_component(bi_plan* p, const uint64_t* in, uint64_t* out, uint8
     for (int r = 0; r < reps + 1; r++) {
         cudaMemsetAsync(p->d_counters, 0, PLAN_KERNELS * sizeof(uint32_t), p->cap);
         cudaEventRecord(e0, p->cap);
-        const cudaStream_t ss[PLAN_KERNELS] = {p->cap, p->cap, p->cap, p->cap, p->cap};
+        cudaStream_t ss[PLAN_KERNELS];
+        for (int k = 0; k < PLAN_KERNELS; k++) ss[k] = p->cap;
         bi_status st = launch_plan_kernels(p, in, out, flags, t, L, ss, comp);
         cudaEventRecord(e1, p->cap);
         cudaEventSynchronize(e1);
@@ -755,7 +764,8 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
     }
     Launch3 L;
     BI_RETURN_IF(prepare_launch(&p, p.tune, &L));
-    const cudaStream_t ss[PLAN_KERNELS] = {s, s, s, s, s};
+    cudaStream_t ss[PLAN_KERNELS];
+    for (int k = 0; k < PLAN_KERNELS; k++) ss[k] = s;
     BI_RETURN_IF(launch_plan_kernels(&p, in, out, flags, p.tune, L, ss));
     // the host staging arrays may be reused once the copies have read them
     e = cudaStreamSynchronize(s);
