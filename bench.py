@@ -208,6 +208,20 @@ def graph_time(fn_on, reps: int = 20):
     return e0.elapsed_time(e1) / reps
 
 
+def whole_job(elapsed_ms: float, per_step_bytes: int, steps: int, world: int, device="cpu"):
+    """(max over ranks of the timed region in ms, whole-job GB/s): every rank
+    runs the full workload on its own GPU (weak scaling, no data exchange), so
+    the job moves world x the per-rank bytes in the slowest rank's time."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(elapsed_ms)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms = float(t.item())
+    return ms, per_step_bytes * steps * world / (ms / 1e3) / 1e9
+
+
 def check(L, st):
     if st != 0:
         raise RuntimeError(f"library call failed: {L.bi_last_error().decode()}")
@@ -739,11 +753,7 @@ def run_ours(args) -> None:
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    t = torch.tensor([start.elapsed_time(stop)], device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    elapsed_ms = float(t.item())
-    value = per_step * args.steps * world / (elapsed_ms / 1e3) / 1e9
+    elapsed_ms, value = whole_job(start.elapsed_time(stop), per_step, args.steps, world, device="cuda")
 
     per_launch = {}
     for (bits, op), e0, e1 in events:

@@ -1,0 +1,67 @@
+"""The bench's multi-rank path on CPU with the gloo backend (world size 2):
+every rank runs the full workload, the timed region is the maximum over
+ranks, and the whole-job rate counts every rank's bytes; the reference arm
+prints from rank 0 only."""
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, q):
+    import torch.distributed as dist
+
+    sys.path.insert(0, REPO)
+    import bench
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        # rank r measured 10 + r ms for a step of 1 GB, 2 steps
+        q.put((rank, bench.whole_job(10.0 + rank, 10**9, 2, world)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_whole_job_rate_is_max_over_ranks_gloo():
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for r in (0, 1):
+        ms, gbs = got[r]
+        assert ms == 11.0                                   # the slower rank's time, on both ranks
+        assert abs(gbs - 2 * 10**9 * 2 / 0.011 / 1e9) < 1e-6   # both ranks' bytes in that time
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, REPO)
+    import bench
+
+    ms, gbs = bench.whole_job(4.0, 3 * 10**9, 5, 1)
+    assert ms == 4.0 and abs(gbs - 3 * 5 / 0.004) < 1e-6
+
+
+def test_reference_arm_prints_from_rank_zero_only():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference", "--steps", "1",
+                        "--warmup", "0"], env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0
+    assert r.stdout.strip() == ""
