@@ -138,6 +138,7 @@ SIGNATURES: dict[str, list] = {
     "bi_server_submit": [_P, _P, _P],
     "bi_server_poll": [_P, _P, _U32, _P],
     "bi_server_release": [_P, _U64],
+    "bi_server_inject_dropped": [_P, _P],
     "bi_server_info": [_P, _P],
     "bi_server_destroy": [_P],
     "bi_server_replay": [_P, _P, _P, _U64, _P, _P, _P],
@@ -489,6 +490,13 @@ class Server:
 
     def release(self, ticket: int):
         _check(lib().bi_server_release(self._h, int(ticket)))
+
+    def inject_dropped(self):
+        """Publish a slot whose contents never arrive (failure injection);
+        returns its ticket, which completes with status 255."""
+        t = ctypes.c_uint64()
+        _check(lib().bi_server_inject_dropped(self._h, ctypes.byref(t)))
+        return t.value
 
     def info(self) -> dict:
         v = (ctypes.c_uint64 * 10)()

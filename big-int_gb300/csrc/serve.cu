@@ -587,6 +587,25 @@ bi_status bi_server_release(bi_server* s, uint64_t ticket) {
     return server_release(s, ticket);
 }
 
+bi_status bi_server_inject_dropped(bi_server* s, uint64_t* ticket) {
+    if (!s) return set_error(BI_EINVAL, "serve: NULL server");
+    if (s->published - s->released >= s->S) return BI_EBUSY;
+    // a slot published with its contents never written: the claiming CTA's
+    // bounded wait for the slot's sequence number runs out
+    const uint64_t seq = s->published;
+    ServeReq& q = s->req[seq & (s->S - 1)];
+    q.seq = seq;
+    q.r = q.r2 = 0;
+    q.end = s->alloc_head;       // no arena space
+    q.op = 0xffffffffu;
+    q.flag = 0;
+    q.state = 1;
+    s->published++;
+    if (ticket) *ticket = seq;
+    server_publish(s);
+    return server_kick(s);
+}
+
 bi_status bi_server_info(const bi_server* s, uint64_t* info) {
     if (!s || !info) return set_error(BI_EINVAL, "serve: NULL argument");
     info[0] = (uint64_t)(uintptr_t)s->out;

@@ -368,6 +368,12 @@ bi_status bi_server_release(bi_server* server, uint64_t ticket);
 /* launches, deferred admissions, lost requests, ring slots, submitted,    */
 /* completed.                                                              */
 bi_status bi_server_info(const bi_server* server, uint64_t* info);
+/* Failure injection on the host: publish one ring slot whose contents are */
+/* never written, as if the host's write had been lost.  The CTA that     */
+/* claims it waits (at most one second) for the slot's sequence number,   */
+/* gives up and completes it with status 255; the other requests go on.   */
+/* The ticket is released like any other.                                 */
+bi_status bi_server_inject_dropped(bi_server* server, uint64_t* ticket);
 /* Stops the loop and frees the server.  A running loop first finishes     */
 /* every request already submitted; requests submitted after the loop     */
 /* ended without a poll or submit to relaunch it are dropped.             */

@@ -292,3 +292,32 @@ def test_destroy_with_requests_in_flight(bigint, setup):
     srv.close()
     with B.Server(pool, _arena(8192)) as srv2:   # the device is usable again
         _run_alone(B, srv2, d[:2])
+
+
+def test_dropped_request_times_out_and_the_loop_goes_on(bigint, oracle, setup):
+    """Failure injection on the host: a published slot whose contents never
+    arrive.  The claiming CTA's bounded wait gives up after a second and
+    completes that request with status 255; requests around it complete
+    normally, during the wait, with the right results."""
+    B = bigint
+    d, _, pool, host = setup
+    with B.Server(pool, _arena(8192), idle_us=3_000_000) as srv:
+        t0 = srv.submit(d[0])
+        tl = srv.inject_dropped()
+        t1 = srv.submit(d[1])
+        done = {}
+        deadline = time.time() + 20
+        while len(done) < 3:
+            assert time.time() < deadline, "no completion for the dropped request"
+            for c in srv.poll():
+                done[int(c["ticket"])] = c
+        assert int(done[tl]["status"]) == 255
+        assert srv.info()["lost"] == 1
+        arena = _host(srv.arena)
+        for t, i in ((t0, 0), (t1, 1)):
+            comp = np.zeros(1, dtype=B.COMPLETION_DTYPE)
+            comp[0] = done[t]
+            res = _collect(B, d[i: i + 1], comp, arena)
+            _check_oracle(B, oracle, d[i: i + 1], host, res)
+        for t in (t0, tl, t1):
+            srv.release(t)
