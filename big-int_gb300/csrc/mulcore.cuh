@@ -31,6 +31,7 @@ struct MulGeom {
     uint32_t m;      // limbs per operand in the caller's type
     uint32_t out_limbs;   // result limbs per instance in the u64 view
     uint32_t out_words;   // result limbs per instance in the caller's type
+    uint32_t S, lgS;      // slices per thread's rows (a power of two; 1 = none)
 };
 
 // The CTA-level multiply of g.ipc instances held in shared memory.  `load`
@@ -38,6 +39,12 @@ struct MulGeom {
 // receives limb x of instance li's result for x < g.out_limbs.  Every thread
 // of the CTA calls it; it ends with the CTA synchronised.  The caller
 // provides g.ipc * g.IS limbs of shared memory and 96 words of scratch.
+//
+// With g.S > 1 each window pair's rows are cut into S slices run by S
+// consecutive lanes, whose partial windows are summed with warp shuffles
+// before the merge: shorter serial carry chains for one instance that has a
+// whole CTA to itself (the serving loop); the extra lanes pass carries
+// through unchanged in the merge's lookahead.
 template <int C, typename Load, typename Store>
 __device__ __forceinline__ void mul_cta(const MulGeom& g, uint64_t* smem, uint32_t* scratch,
                                         const FastDiv& lpdiv, Load load, Store store) {
@@ -66,9 +73,12 @@ __device__ __forceinline__ void mul_cta(const MulGeom& g, uint64_t* smem, uint32
     }
     __syncthreads();
 
-    const uint32_t li = tid / g.tpi;
-    const uint32_t rank = tid - li * g.tpi;
+    const uint32_t grp = tid >> g.lgS;            // (instance, rank) group of S lanes
+    const uint32_t sl = tid & (g.S - 1);          // slice within the group
+    const uint32_t li = grp / g.tpi;
+    const uint32_t rank = grp - li * g.tpi;
     const bool active = li < g.ipc;
+    const bool merger = active && sl == 0;
     uint64_t R[C + 2], R1[C + 2];
 #pragma unroll
     for (int e = 0; e < C + 2; e++) { R[e] = 0; R1[e] = 0; }
@@ -96,7 +106,10 @@ __device__ __forceinline__ void mul_cta(const MulGeom& g, uint64_t* smem, uint32
             a2 = u2 * C; b2 = Lp;
         }
         const uint32_t nblk = nwin_half + 1;
-        for (uint32_t blk = 0; blk < nblk; blk++) {
+        const uint32_t per = (nblk + g.S - 1) >> g.lgS;
+        const uint32_t b_lo = sl * per < nblk ? sl * per : nblk;
+        const uint32_t b_hi = b_lo + per < nblk ? b_lo + per : nblk;
+        for (uint32_t blk = b_lo; blk < b_hi; blk++) {
             if (blk == nblk1) {
 #pragma unroll
                 for (int e = 0; e < C + 2; e++) { R1[e] = R[e]; R[e] = 0; }
@@ -125,11 +138,28 @@ __device__ __forceinline__ void mul_cta(const MulGeom& g, uint64_t* smem, uint32
             row_mac8<2>(R, av[6], ext);
             row_mac8<1>(R, av[7], ext);
         }
+        if (b_hi <= nblk1) {   // the slice ended among window w1's rows
+#pragma unroll
+            for (int e = 0; e < C + 2; e++) { R1[e] = R[e]; R[e] = 0; }
+        }
+    }
+    // sum the S slices of each window pair onto slice 0
+    for (uint32_t off = g.S >> 1; off > 0; off >>= 1) {
+        uint64_t o1[C + 2], o2[C + 2];
+#pragma unroll
+        for (int e = 0; e < C + 2; e++) {
+            o1[e] = __shfl_down_sync(0xffffffffu, R1[e], off);
+            o2[e] = __shfl_down_sync(0xffffffffu, R[e], off);
+        }
+        if (sl < off) {
+            add10(R1, o1);
+            add10(R, o2);
+        }
     }
     __syncthreads();   // every thread is done reading a_s / b_s
 
     // ---- window results into shared memory (over the operand area)
-    if (active) {
+    if (merger) {
         uint64_t* racc = smem + (size_t)li * g.IS;
 #pragma unroll
         for (int e = 0; e < C + 2; e++) {
@@ -141,9 +171,9 @@ __device__ __forceinline__ void mul_cta(const MulGeom& g, uint64_t* smem, uint32
 
     // ---- merge: thread takes windows 2*rank and 2*rank+1; D_u = P_u + O_{u-1}
     uint64_t D0[C], D1[C];
-    uint32_t gq = 0, pq = 0;
+    uint32_t gq = 0, pq = active ? 1u : 0u;   // slice lanes pass carries through
     uint32_t g0 = 0, p0 = 0;
-    if (active) {
+    if (merger) {
         const uint64_t* racc = smem + (size_t)li * g.IS;
         const uint32_t u0 = 2 * rank, u1 = u0 + 1;
         uint64_t o0 = 0, o1 = 0;
@@ -185,9 +215,9 @@ __device__ __forceinline__ void mul_cta(const MulGeom& g, uint64_t* smem, uint32
         gq = g1 | (p1 & g0);
         pq = p0 & p1;
     }
-    const uint32_t cin = block_carry_in(gq, pq, !active || rank == 0, scratch);
+    const uint32_t cin = block_carry_in(gq, pq, !active || (rank == 0 && sl == 0), scratch);
 
-    if (active) {
+    if (merger) {
         uint32_t c = cin;
 #pragma unroll
         for (int e = 0; e < C; e++) {
@@ -234,10 +264,24 @@ __host__ __device__ inline MulGeom mul_geometry(uint32_t L, bool full, uint32_t 
     if ((g.IS / 2) % 2 == 0) g.IS += 2;         // odd 16-byte stride spreads banks across instances
     g.out_limbs = full ? 2 * L : L;
     g.out_words = g.out_limbs;
+    g.S = 1;
+    g.lgS = 0;
     return g;
 }
 
-__host__ __device__ inline uint32_t mul_threads(const MulGeom& g) { return (g.ipc * g.tpi + 31) / 32 * 32; }
+// One instance with its rows cut into S slices: S = the largest power of two
+// up to `threads` / tpi and up to one row block per slice.
+__host__ __device__ inline MulGeom mul_geometry_single_sliced(uint32_t L, bool full, uint32_t threads) {
+    MulGeom g = mul_geometry(L, full, 1);
+    const uint32_t nblk = g.Lp / MUL_C + 1;
+    uint32_t lg = 0;
+    while (lg < 5 && (g.tpi << (lg + 1)) <= threads && (2u << lg) <= nblk) lg++;
+    g.S = 1u << lg;
+    g.lgS = lg;
+    return g;
+}
+
+__host__ __device__ inline uint32_t mul_threads(const MulGeom& g) { return (g.ipc * g.tpi * g.S + 31) / 32 * 32; }
 __host__ __device__ inline size_t mul_smem_bytes(const MulGeom& g) { return (size_t)g.ipc * g.IS * 8 + 3 * 32 * 4; }
 
 }  // namespace bi

@@ -221,7 +221,7 @@ __global__ void __launch_bounds__(SERVE_CTA, 2) serve_kernel(const ServeArgs A) 
                 }
             } else if (d.op == BI_OP_MUL || d.op == BI_OP_MULFULL) {
                 const bool full = d.op == BI_OP_MULFULL;
-                const MulGeom g = mul_geometry(d.m, full, 1);
+                const MulGeom g = mul_geometry_single_sliced(d.m, full, SERVE_CTA);
                 uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + (size_t)g.ipc * g.IS);
                 const FastDiv lpdiv(g.Lp);
                 const uint32_t m = d.m, outl = full ? 2 * d.m : d.m;
