@@ -97,6 +97,10 @@ SIGNATURES: dict[str, list] = {
     "bi_max_limbs_mul_u32": [],
     "bi_div_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
     "bi_div_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
+    "bi_div_shinv_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
+    "bi_div_shinv_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
+    "bi_div_long_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
+    "bi_div_long_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
     "bi_host_div_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64],
     "bi_host_div_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64],
     "bi_max_limbs_div_u64": [],
@@ -254,8 +258,10 @@ def mulfull(a, b, out=None, stream=None):
     return out
 
 
-def div(u, v, q=None, r=None, status=None, stream=None):
-    """(q, r, status) per row: q = floor(u / v), r = u mod v; status 1 = zero divisor."""
+def div(u, v, q=None, r=None, status=None, stream=None, method="auto"):
+    """(q, r, status) per row: q = floor(u / v), r = u mod v; status 1 = zero divisor.
+    method: "auto" (bi_div_*), "shinv" (the shifted inverse at every size,
+    bi_div_shinv_*) or "long" (long division, bi_div_long_*)."""
     import torch
 
     _dev2d(u, "u"), _dev2d(v, "v")
@@ -267,8 +273,11 @@ def div(u, v, q=None, r=None, status=None, stream=None):
         r = torch.empty((n, mv), dtype=u.dtype, device=u.device)
     if status is None:
         status = torch.empty(n, dtype=torch.uint8, device=u.device)
-    _check(getattr(lib(), f"bi_div_{_wsuffix(u)}")(u.data_ptr(), v.data_ptr(), q.data_ptr(), r.data_ptr(),
-                                                  status.data_ptr(), mu, mv, n, _stream_ptr(stream)))
+    if method not in ("auto", "shinv", "long"):
+        raise ValueError(f"div: unknown method {method!r}")
+    name = f"bi_div_{_wsuffix(u)}" if method == "auto" else f"bi_div_{method}_{_wsuffix(u)}"
+    _check(getattr(lib(), name)(u.data_ptr(), v.data_ptr(), q.data_ptr(), r.data_ptr(),
+                                status.data_ptr(), mu, mv, n, _stream_ptr(stream)))
     return q, r, status
 
 

@@ -12,14 +12,15 @@
 //     size mix keeps the warps busy;
 //   * multiplications are bucketed by padded size; a persistent CTA takes a
 //     bucket item (as many instances as fit one CTA, mulcore.cuh);
-//   * divisions go one per CTA to persistent kernels (divcore.cuh), one per
-//     size class of dividend -- under 64 limbs on 64-thread CTAs, under 256
-//     on 128-thread CTAs, under 1024 on 256-thread CTAs, the rest on
-//     512-thread CTAs -- each sized for the shared memory of its own largest
-//     division, so small divisions run many CTAs per SM instead of one and
-//     the largest get as many warps as an SM's registers allow; most
-//     expensive first within a class.
-// The six persistent kernels run concurrently on forked streams; the fork,
+//   * divisions go to persistent kernels by divisor size class: schoolbook
+//     long division (divsmall.cuh) on one thread per instance for divisors
+//     up to 4, 8 and 16 limbs, on one warp per instance up to 32, 64, ...,
+//     1024 limbs (the register arrays sized for the class), and the shifted
+//     inverse (divcore.cuh) on one 512-thread CTA per instance above; most
+//     expensive first within a class.  A batch holds many divisions of each
+//     class, where long division's throughput wins (uniform batches choose
+//     per call, div.cu).
+// The persistent kernels run concurrently on forked streams; the fork,
 // the launches, the counter reset and the join are captured once into a CUDA
 // graph and replayed by every bi_plan_execute.  Work is handed out with one
 // atomic counter per kernel (no waiting on other CTAs).
@@ -29,6 +30,7 @@
 #include <vector>
 
 #include "divcore.cuh"
+#include "divsmall.cuh"
 #include "mulcore.cuh"
 #include "warpops.cuh"
 
@@ -123,12 +125,70 @@ batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
     }
 }
 
-// division size classes by dividend limbs: < 64, < 256, < 1024, the rest
-constexpr int DIV_CLASSES = 4;
-constexpr int DIV_CLASS_THREADS[DIV_CLASSES] = {64, 128, 256, 512};
+// division classes by divisor limbs: long division on threads (divisors up
+// to 4, 8, 16 limbs), on warps (up to 32, 64, ..., 1024 limbs), the shifted
+// inverse on 512-thread CTAs above
+constexpr int DIV_THREAD_CLASSES = 3, DIV_WARP_CLASSES = 6;
+constexpr int DIV_CTA_CLASS = DIV_THREAD_CLASSES + DIV_WARP_CLASSES;
+constexpr int DIV_CLASSES = DIV_CTA_CLASS + 1;
+constexpr int DIV_CTA_THREADS = 512;
 constexpr int PLAN_KERNELS = 2 + DIV_CLASSES;   // add/sub, multiply, one per division class
 
-static inline int div_class(uint32_t mu) { return mu < 64 ? 0 : mu < 256 ? 1 : mu < 1024 ? 2 : 3; }
+static inline int div_class(uint32_t mv) {
+    if (mv <= 4) return 0;
+    if (mv <= 8) return 1;
+    if (mv <= 16) return 2;
+    if (mv > (uint32_t)DIV_WARP_MAX_MV) return DIV_CTA_CLASS;
+    int c = DIV_THREAD_CLASSES;
+    for (uint32_t cap = 32; cap < mv; cap *= 2) c++;
+    return c;
+}
+
+template <int MX>
+__global__ void __launch_bounds__(DIV_THREAD_CTA)
+batch_divthread_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                       uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, 32u);   // 32 instances a warp
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count) break;
+        const uint32_t idx = base + lane;
+        if (idx >= count) continue;
+        const bi_desc d = descs[list[idx]];
+        const uint64_t* u = in + d.a;
+        const uint64_t* v = in + d.b;
+        uint64_t* q = out + d.r;
+        uint64_t* r = out + d.r2;
+        const uint8_t st = div_thread<MX>(
+            d.m, d.mb, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
+            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; });
+        if (flags) flags[d.flag] = st;
+    }
+}
+
+template <int VPL>
+__global__ void __launch_bounds__(DIV_WARP_CTA)
+batch_divwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                     uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(counter, 1u);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= count) break;
+        const bi_desc d = descs[list[idx]];
+        const uint64_t* u = in + d.a;
+        const uint64_t* v = in + d.b;
+        uint64_t* q = out + d.r;
+        uint64_t* r = out + d.r2;
+        const uint8_t st = div_warp<VPL>(
+            d.m, d.mb, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
+            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; });
+        if (flags && lane == 0) flags[d.flag] = st;
+    }
+}
 
 // At most 128 registers a thread, so 512 / THREADS CTAs fit an SM's register file.
 template <int THREADS>
@@ -221,7 +281,7 @@ static size_t mul_smem_for(const bi_plan* p, int ipc_div) {
 
 // Division order: by size class, then most expensive first.
 static bool div_before(const bi_desc& x, const bi_desc& y) {
-    const int cx = div_class(x.m), cy = div_class(y.m);
+    const int cx = div_class(x.mb), cy = div_class(y.mb);
     if (cx != cy) return cx < cy;
     return (uint64_t)x.m * x.mb > (uint64_t)y.m * y.mb;
 }
@@ -236,9 +296,9 @@ static void div_classes(bi_plan* p, const bi_desc* descs, const uint32_t* div, u
     }
     for (uint32_t k = 0; k < n; k++) {
         const bi_desc& d = descs[div[k]];
-        const int c = div_class(d.m);
+        const int c = div_class(d.mb);
         if (p->n_divc[c]++ == 0) p->div_off[c] = k;
-        p->divc_smem[c] = std::max(p->divc_smem[c], div_smem_bytes(div_geom(d.m, d.mb, 8)));
+        if (c == DIV_CTA_CLASS) p->divc_smem[c] = std::max(p->divc_smem[c], div_smem_bytes(div_geom(d.m, d.mb, 8)));
         p->div_smem = std::max(p->div_smem, p->divc_smem[c]);
     }
 }
@@ -250,15 +310,30 @@ struct Launch3 {
     size_t smem[PLAN_KERNELS];
 };
 
-template <int THREADS>
-static bi_status prepare_div_class(uint32_t n, size_t smem, int sms, unsigned* grid) {
+static bi_status grid_for(const void* k, int threads, size_t smem, uint64_t work_ctas, int sms, unsigned* grid) {
     int occ = 1;
-    auto k = batch_div_kernel<THREADS>;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, THREADS, smem) != cudaSuccess)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, smem) != cudaSuccess)
         return set_error(BI_ECUDA, "batch div kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
-    *grid = (unsigned)std::min<uint64_t>(n, (uint64_t)sms * (occ < 1 ? 1 : occ));
+    *grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(work_ctas, (uint64_t)sms * (occ < 1 ? 1 : occ)));
     return BI_OK;
+}
+
+// The kernel of division class c (host-side function pointer) and its CTA width.
+static const void* div_class_kernel(int c, int* threads) {
+    *threads = c < DIV_THREAD_CLASSES ? DIV_THREAD_CTA : c < DIV_CTA_CLASS ? DIV_WARP_CTA : DIV_CTA_THREADS;
+    switch (c) {
+    case 0: return (const void*)batch_divthread_kernel<4>;
+    case 1: return (const void*)batch_divthread_kernel<8>;
+    case 2: return (const void*)batch_divthread_kernel<16>;
+    case 3: return (const void*)batch_divwarp_kernel<1>;
+    case 4: return (const void*)batch_divwarp_kernel<2>;
+    case 5: return (const void*)batch_divwarp_kernel<4>;
+    case 6: return (const void*)batch_divwarp_kernel<8>;
+    case 7: return (const void*)batch_divwarp_kernel<16>;
+    case 8: return (const void*)batch_divwarp_kernel<32>;
+    default: return (const void*)batch_div_kernel<DIV_CTA_THREADS>;
+    }
 }
 
 // Grid sizes and shared memory of the kernels for tuning t; sets the
@@ -279,14 +354,19 @@ static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
             return set_error(BI_ECUDA, "batch mul kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
         L->grid[1] = (unsigned)std::min<uint64_t>(p->n_items, (uint64_t)sms * (occ < 1 ? 1 : occ));
     }
-    if (p->n_divc[0]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[0]>(p->n_divc[0], L->smem[2], sms, &L->grid[2]));
-    if (p->n_divc[1]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[1]>(p->n_divc[1], L->smem[3], sms, &L->grid[3]));
-    if (p->n_divc[2]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[2]>(p->n_divc[2], L->smem[4], sms, &L->grid[4]));
-    if (p->n_divc[3]) BI_RETURN_IF(prepare_div_class<DIV_CLASS_THREADS[3]>(p->n_divc[3], L->smem[5], sms, &L->grid[5]));
+    for (int c = 0; c < DIV_CLASSES; c++) {
+        const uint64_t n = p->n_divc[c];
+        if (!n) continue;
+        int threads = 0;
+        const void* k = div_class_kernel(c, &threads);
+        // instances per CTA: one a thread, one a warp, one a CTA
+        const uint64_t per = c < DIV_THREAD_CLASSES ? (uint64_t)threads : c < DIV_CTA_CLASS ? (uint64_t)threads / 32 : 1;
+        BI_RETURN_IF(grid_for(k, threads, L->smem[2 + c], (n + per - 1) / per, sms, &L->grid[2 + c]));
+    }
     return BI_OK;
 }
 
-// s[k] is the stream of kernel k (add/sub, multiply, division classes 0..3).
+// s[k] is the stream of kernel k (add/sub, multiply, then the division classes).
 static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags,
                                      const BatchTune& t, const Launch3& L, const cudaStream_t* s,
                                      int comps = COMP_ALL) {
@@ -310,24 +390,27 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
     }
     if (comps & COMP_DIV) {
         // the largest class first: its divisions take longest
-        if (p->n_divc[3]) {
-            batch_div_kernel<DIV_CLASS_THREADS[3]><<<L.grid[5], DIV_CLASS_THREADS[3], L.smem[5], s[5]>>>(
-                p->d_descs, p->d_div + p->div_off[3], p->n_divc[3], p->d_counters + 5, in, out, flags);
-            BI_RETURN_IF(check_launch("batch div kernel"));
-        }
-        if (p->n_divc[2]) {
-            batch_div_kernel<DIV_CLASS_THREADS[2]><<<L.grid[4], DIV_CLASS_THREADS[2], L.smem[4], s[4]>>>(
-                p->d_descs, p->d_div + p->div_off[2], p->n_divc[2], p->d_counters + 4, in, out, flags);
-            BI_RETURN_IF(check_launch("batch div kernel"));
-        }
-        if (p->n_divc[1]) {
-            batch_div_kernel<DIV_CLASS_THREADS[1]><<<L.grid[3], DIV_CLASS_THREADS[1], L.smem[3], s[3]>>>(
-                p->d_descs, p->d_div + p->div_off[1], p->n_divc[1], p->d_counters + 3, in, out, flags);
-            BI_RETURN_IF(check_launch("batch div kernel"));
-        }
-        if (p->n_divc[0]) {
-            batch_div_kernel<DIV_CLASS_THREADS[0]><<<L.grid[2], DIV_CLASS_THREADS[0], L.smem[2], s[2]>>>(
-                p->d_descs, p->d_div + p->div_off[0], p->n_divc[0], p->d_counters + 2, in, out, flags);
+        for (int c = DIV_CLASSES - 1; c >= 0; c--) {
+            const uint32_t n = p->n_divc[c];
+            if (!n) continue;
+            const uint32_t* list = p->d_div + p->div_off[c];
+            uint32_t* ctr = p->d_counters + 2 + c;
+            const unsigned grid = L.grid[2 + c];
+            cudaStream_t st = s[2 + c];
+            switch (c) {
+            case 0: batch_divthread_kernel<4><<<grid, DIV_THREAD_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 1: batch_divthread_kernel<8><<<grid, DIV_THREAD_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 2: batch_divthread_kernel<16><<<grid, DIV_THREAD_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 3: batch_divwarp_kernel<1><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 4: batch_divwarp_kernel<2><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 5: batch_divwarp_kernel<4><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 6: batch_divwarp_kernel<8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 7: batch_divwarp_kernel<16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 8: batch_divwarp_kernel<32><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            default:
+                batch_div_kernel<DIV_CTA_THREADS><<<grid, DIV_CTA_THREADS, L.smem[2 + c], st>>>(p->d_descs, list, n, ctr,
+                                                                                             in, out, flags);
+            }
             BI_RETURN_IF(check_launch("batch div kernel"));
         }
     }
@@ -488,7 +571,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     if (st == BI_OK) st = dev_upload(&p->d_div, div, p->cap);
     if (st == BI_OK) st = dev_upload(&p->d_items, items, p->cap);
     if (st == BI_OK) {
-        std::vector<uint32_t> zeros(8, 0);
+        std::vector<uint32_t> zeros(PLAN_KERNELS, 0);
         st = dev_upload(&p->d_counters, zeros, p->cap);
     }
     if (st == BI_OK && cudaStreamSynchronize(p->cap) != cudaSuccess) st = set_error(BI_ECUDA, "plan upload failed");
@@ -641,6 +724,7 @@ constexpr size_t NA_DIV_OFF = NA_MUL_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(ui
 constexpr size_t NA_ITEM_OFF = NA_DIV_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(uint32_t);
 constexpr size_t NA_CNT_OFF = NA_ITEM_OFF + (size_t)NOALLOC_MAX_DESCS * sizeof(MulItem);
 constexpr size_t NOALLOC_SCRATCH_BYTES = NA_CNT_OFF + 256;
+static_assert(PLAN_KERNELS * sizeof(uint32_t) <= 256, "plan counters outgrow their scratch slot");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_SCRATCH_BYTES];
 

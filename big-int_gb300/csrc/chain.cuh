@@ -54,6 +54,45 @@ BI_DEF_SUB8(chain_sub8, uint32_t, "u32", "r")
 #undef BI_CH_OUTS
 #undef BI_CH_INS
 
+// x = x - y - c over N = 1, 2 or 4 limbs of 64 bits; returns the borrow out.
+__device__ __forceinline__ uint32_t chain_sub_n(uint64_t (&x)[1], const uint64_t (&y)[1], uint32_t c) {
+    uint32_t bo;
+    asm("{\n\t.reg .u32 t;\n\tsub.cc.u32 t, 0, %3;\n\tsubc.cc.u64 %0, %0, %2;\n\tsubc.u32 %1, 0, 0;\n\t}"
+        : "+l"(x[0]), "=r"(bo)
+        : "l"(y[0]), "r"(c));
+    return bo & 1u;
+}
+__device__ __forceinline__ uint32_t chain_sub_n(uint64_t (&x)[2], const uint64_t (&y)[2], uint32_t c) {
+    uint32_t bo;
+    asm("{\n\t.reg .u32 t;\n\tsub.cc.u32 t, 0, %5;\n\tsubc.cc.u64 %0, %0, %3;\n\tsubc.cc.u64 %1, %1, %4;\n\t"
+        "subc.u32 %2, 0, 0;\n\t}"
+        : "+l"(x[0]), "+l"(x[1]), "=r"(bo)
+        : "l"(y[0]), "l"(y[1]), "r"(c));
+    return bo & 1u;
+}
+__device__ __forceinline__ uint32_t chain_sub_n(uint64_t (&x)[4], const uint64_t (&y)[4], uint32_t c) {
+    uint32_t bo;
+    asm("{\n\t.reg .u32 t;\n\tsub.cc.u32 t, 0, %9;\n\tsubc.cc.u64 %0, %0, %5;\n\tsubc.cc.u64 %1, %1, %6;\n\t"
+        "subc.cc.u64 %2, %2, %7;\n\tsubc.cc.u64 %3, %3, %8;\n\tsubc.u32 %4, 0, 0;\n\t}"
+        : "+l"(x[0]), "+l"(x[1]), "+l"(x[2]), "+l"(x[3]), "=r"(bo)
+        : "l"(y[0]), "l"(y[1]), "l"(y[2]), "l"(y[3]), "r"(c));
+    return bo & 1u;
+}
+// Any N that is 1, 2, 4 or a multiple of 8: blocks of 8 pass the borrow on.
+template <int N>
+__device__ __forceinline__ uint32_t chain_sub(uint64_t (&x)[N], const uint64_t (&y)[N], uint32_t c) {
+    if constexpr (N == 1 || N == 2 || N == 4) {
+        return chain_sub_n(x, y, c);
+    } else {
+        static_assert(N % 8 == 0, "chain_sub: N must be 1, 2, 4 or a multiple of 8");
+#pragma unroll
+        for (int b = 0; b < N / 8; b++)
+            c = chain_sub8(*reinterpret_cast<uint64_t(*)[8]>(&x[8 * b]),
+                           *reinterpret_cast<const uint64_t(*)[8]>(&y[8 * b]), c);
+        return c;
+    }
+}
+
 // The carry out alone (x and y unchanged): the same chain on copies.
 template <typename T>
 __device__ __forceinline__ uint32_t chain_add8_cout(const T (&x)[8], const T (&y)[8], uint32_t c) {

@@ -24,7 +24,15 @@
 //   4. r is shifted back right by s bits.
 // The estimate is exact or one short in every case tested; a bound of
 // DIV_MAX_CORRECTIONS steps on each side turns anything else into status 2.
+//
+// Small and medium divisors take another route to the same unique (q, r):
+// schoolbook long division (divsmall.cuh) on one thread per instance up to
+// DIV_THREAD_MAX_MV 64-bit limbs and on one warp per instance up to
+// DIV_WARP_MAX_MV, where its K (MU - K + 1) limb products and no barriers
+// cost less than a CTA running the steps above (div_use_long holds the
+// measured crossover, which depends on the batch size too).
 #include "divcore.cuh"
+#include "divsmall.cuh"
 
 namespace bi {
 
@@ -69,11 +77,81 @@ div_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, 
 
 // ---------------------------------------------------------------------------
 
-constexpr uint32_t DIV_MAX_MU64 = 2048;   // dividend limbs (u64 view) per instance
+// One thread per instance: long division for divisors of at most MX limbs
+// (divsmall.cuh).
+template <typename T, int MX>
+__global__ void __launch_bounds__(DIV_THREAD_CTA)
+div_thread_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
+                  uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
+    const uint32_t MU = sizeof(T) == 8 ? mu : (mu + 1) / 2, MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    for (uint64_t inst = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; inst < n;
+         inst += (uint64_t)gridDim.x * blockDim.x) {
+        const T* ui = u + inst * mu;
+        const T* vi = v + inst * mv;
+        T* qi = q + inst * mu;
+        T* ri = r + inst * mv;
+        const uint8_t st = div_thread<MX>(
+            MU, MV, [&](uint32_t i) { return limb64(ui, mu, i); }, [&](uint32_t i) { return limb64(vi, mv, i); },
+            [&](uint32_t i, uint64_t x) { put_limb64(qi, mu, i, x); },
+            [&](uint32_t i, uint64_t x) { put_limb64(ri, mv, i, x); });
+        if (status) status[inst] = st;
+    }
+}
+
+template <typename T>
+static void launch_div_thread(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
+                              uint64_t n, cudaStream_t s) {
+    const uint32_t MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    const uint64_t blocks = (n + DIV_THREAD_CTA - 1) / DIV_THREAD_CTA;
+    const unsigned grid = (unsigned)(blocks < (1u << 20) ? blocks : (1u << 20));
+    if (MV <= 2) div_thread_kernel<T, 2><<<grid, DIV_THREAD_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 4) div_thread_kernel<T, 4><<<grid, DIV_THREAD_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 8) div_thread_kernel<T, 8><<<grid, DIV_THREAD_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else div_thread_kernel<T, 16><<<grid, DIV_THREAD_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+}
+
+// One warp per instance: long division for divisors of at most 32 VPL limbs
+// (divsmall.cuh).
+template <typename T, int VPL>
+__global__ void __launch_bounds__(DIV_WARP_CTA)
+div_warp_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
+                uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
+    const uint32_t MU = sizeof(T) == 8 ? mu : (mu + 1) / 2, MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    const uint64_t warps = (uint64_t)gridDim.x * (DIV_WARP_CTA / 32);
+    for (uint64_t inst = (uint64_t)blockIdx.x * (DIV_WARP_CTA / 32) + threadIdx.x / 32; inst < n; inst += warps) {
+        const T* ui = u + inst * mu;
+        const T* vi = v + inst * mv;
+        T* qi = q + inst * mu;
+        T* ri = r + inst * mv;
+        const uint8_t st = div_warp<VPL>(
+            MU, MV, [&](uint32_t i) { return limb64(ui, mu, i); }, [&](uint32_t i) { return limb64(vi, mv, i); },
+            [&](uint32_t i, uint64_t x) { put_limb64(qi, mu, i, x); },
+            [&](uint32_t i, uint64_t x) { put_limb64(ri, mv, i, x); });
+        if (status && (threadIdx.x & 31) == 0) status[inst] = st;
+    }
+}
+
+template <typename T>
+static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
+                            uint64_t n, cudaStream_t s) {
+    const uint32_t MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    constexpr uint32_t per_cta = DIV_WARP_CTA / 32;
+    const uint64_t blocks = (n + per_cta - 1) / per_cta;
+    const unsigned grid = (unsigned)(blocks < (1u << 20) ? blocks : (1u << 20));
+    if (MV <= 32) div_warp_kernel<T, 1><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 64) div_warp_kernel<T, 2><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 128) div_warp_kernel<T, 4><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 256) div_warp_kernel<T, 8><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 512) div_warp_kernel<T, 16><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else div_warp_kernel<T, 32><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+}
+
+constexpr uint32_t DIV_MAX_MU64 = 2048;
+constexpr int DIV_AUTO = 0, DIV_SHINV = 1, DIV_LONG = 2;   // method of div_entry   // dividend limbs (u64 view) per instance
 
 template <typename T>
 static bi_status div_entry(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
-                           uint64_t n, bi_stream s) {
+                           uint64_t n, bi_stream s, int method = DIV_AUTO) {
     if (n == 0) return BI_OK;
     if (mu == 0 || mv == 0) return set_error(BI_EINVAL, "mu and mv must be >= 1");
     if (mv > mu) return set_error(BI_EINVAL, "divisor limbs mv=%u exceed dividend limbs mu=%u", mv, mu);
@@ -82,6 +160,17 @@ static bi_status div_entry(const T* u, const T* v, T* q, T* r, uint8_t* status, 
         (uintptr_t)r % sizeof(T))
         return set_error(BI_EINVAL, "buffers must be aligned to the limb size");
     const DivGeom g = div_geom(mu, mv, (int)sizeof(T));
+    if (method == DIV_LONG && g.MV > (uint32_t)DIV_WARP_MAX_MV)
+        return set_error(BI_EUNSUPPORTED, "div_long: divisor of %u limbs above %d 64-bit limbs", mv, DIV_WARP_MAX_MV);
+    if (method != DIV_SHINV && g.MV <= (uint32_t)DIV_THREAD_MAX_MV) {
+        launch_div_thread(u, v, q, r, status, mu, mv, n, (cudaStream_t)s);
+        return check_launch("div thread kernel");
+    }
+    if (method != DIV_SHINV && g.MV <= (uint32_t)DIV_WARP_MAX_MV &&
+        (method == DIV_LONG || div_use_long(g.MV, n, num_sms()))) {
+        launch_div_warp(u, v, q, r, status, mu, mv, n, (cudaStream_t)s);
+        return check_launch("div warp kernel");
+    }
     if (g.MU > DIV_MAX_MU64) return set_error(BI_EUNSUPPORTED, "div: dividend of %u limbs above the supported size", mu);
     const size_t smem = div_smem_bytes(g);
     if (smem > 227 * 1024) return set_error(BI_EUNSUPPORTED, "div: sizes need too much shared memory");
@@ -110,6 +199,23 @@ bi_status bi_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t
 bi_status bi_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r, uint8_t* status,
                      uint32_t mu, uint32_t mv, uint64_t n, bi_stream s) {
     return div_entry<uint32_t>(u, v, q, r, status, mu, mv, n, s);
+}
+
+bi_status bi_div_shinv_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r, uint8_t* status,
+                           uint32_t mu, uint32_t mv, uint64_t n, bi_stream s) {
+    return div_entry<uint64_t>(u, v, q, r, status, mu, mv, n, s, DIV_SHINV);
+}
+bi_status bi_div_shinv_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r, uint8_t* status,
+                           uint32_t mu, uint32_t mv, uint64_t n, bi_stream s) {
+    return div_entry<uint32_t>(u, v, q, r, status, mu, mv, n, s, DIV_SHINV);
+}
+bi_status bi_div_long_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r, uint8_t* status,
+                          uint32_t mu, uint32_t mv, uint64_t n, bi_stream s) {
+    return div_entry<uint64_t>(u, v, q, r, status, mu, mv, n, s, DIV_LONG);
+}
+bi_status bi_div_long_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r, uint8_t* status,
+                          uint32_t mu, uint32_t mv, uint64_t n, bi_stream s) {
+    return div_entry<uint32_t>(u, v, q, r, status, mu, mv, n, s, DIV_LONG);
 }
 
 }  // extern "C"

@@ -1,0 +1,382 @@
+// divsmall.cuh -- division of one instance by one thread, for divisors of at
+// most 16 64-bit limbs: schoolbook long division (Knuth, TAOCP vol. 2,
+// 4.3.1, Algorithm D) with 2-by-1 quotient estimates (Moller and Granlund's
+// reciprocal, divcore.cuh).  The quotient and remainder of u / v are unique,
+// so the results are the ones the shifted-inverse division (divcore.cuh, the
+// reference's algorithm) gives; what changes is the cost.  Long division does
+// (MU - K + 1) K limb products for a K-limb divisor, about one multiply's
+// worth, where the shifted inverse does several multiplies' worth plus a
+// barrier per block operation -- at these sizes the barriers and the CTA
+// bookkeeping are the whole cost, and one thread per instance has none.
+//
+// Registers: the divisor D and the (MX + 1)-limb window of the running
+// remainder are register arrays of compile-time size MX with compile-time
+// indices only.  The divisor is right-aligned in D (its K limbs at the top,
+// zeros below), which divides u B^(MX-K) by v B^(MX-K): the same quotient, a
+// remainder scaled by B^(MX-K), with no index that depends on K.
+#pragma once
+
+#include "chain.cuh"
+#include "divcore.cuh"
+
+namespace bi {
+
+constexpr int DIV_THREAD_MAX_MV = 16;   // 64-bit divisor limbs handled by div_thread
+constexpr int DIV_THREAD_CTA = 64;      // threads per CTA of the one-thread-per-instance kernels
+constexpr int DIV_WARP_MAX_MV = 1024;   // 64-bit divisor limbs handled by div_warp
+constexpr int DIV_WARP_CTA = 128;       // threads per CTA of the one-warp-per-instance kernels
+
+// Long division on warps or the shifted inverse on CTAs, for a batch of n
+// instances with MV-limb divisors (64-bit limbs) on a GPU of `sms` SMs.
+// Long division does fewer limb products but runs one quotient limb after
+// another (about 0.5 us per limb at 64 limbs, 1.5 us at 1024), so with few
+// instances one CTA per instance finishes sooner; past a few instances per SM
+// the warps' throughput wins.  Measured crossovers (dividend 2 MV limbs,
+// GB300): long division always up to 128 limbs; above that once n exceeds
+// 2, 3 and 6 instances per SM for divisors up to 256, 512 and 1024 limbs.
+__host__ __device__ inline bool div_use_long(uint32_t MV, uint64_t n, int sms) {
+    if (MV <= (uint32_t)DIV_THREAD_MAX_MV || MV <= 128) return true;
+    if (MV > (uint32_t)DIV_WARP_MAX_MV) return false;
+    const uint64_t per_sm = MV <= 256 ? 2 : MV <= 512 ? 3 : 6;
+    return n > per_sm * (uint64_t)sms;
+}
+
+// One instance: u (MU 64-bit limbs through load_u), v (MV <= MX limbs through
+// load_v); writes MU quotient limbs and MV remainder limbs.  Returns the
+// status: 0, or 1 when v == 0 (then q = r = 0).
+template <int MX, typename LoadU, typename LoadV, typename StoreQ, typename StoreR>
+__device__ __forceinline__ uint8_t div_thread(uint32_t MU, uint32_t MV, LoadU load_u, LoadV load_v, StoreQ store_q,
+                                              StoreR store_r) {
+    static_assert(MX >= 2, "the quotient estimate reads two divisor limbs");
+    uint64_t D[MX];
+#pragma unroll
+    for (int k = 0; k < MX; k++) {
+        const int i = k - (MX - (int)MV);
+        D[k] = i >= 0 ? load_v((uint32_t)i) : 0;
+    }
+    // move the top nonzero limb to D[MX-1]: K = the divisor's precision
+    int K = (int)MV;
+    for (int z = 0; z < MX && D[MX - 1] == 0; z++) {
+#pragma unroll
+        for (int k = MX - 1; k > 0; k--) D[k] = D[k - 1];
+        D[0] = 0;
+        K--;
+    }
+    if (K <= 0) {
+        for (uint32_t i = 0; i < MU; i++) store_q(i, 0);
+        for (uint32_t i = 0; i < MV; i++) store_r(i, 0);
+        return 1;
+    }
+    const int s = __clzll((long long)D[MX - 1]);
+    const int rs = 63 - s;   // x >> (64 - s) written as (x >> 1) >> rs: 0 when s == 0
+#pragma unroll
+    for (int k = MX - 1; k > 0; k--) D[k] = (D[k] << s) | ((D[k - 1] >> 1) >> rs);
+    D[0] <<= s;
+    const int zl = MX - K;   // zero limbs below the divisor
+
+    // the shifted dividend: sh(t) = limb t of u 2^s, t in [0, MU]
+    auto raw = [&](int t) -> uint64_t { return (t >= 0 && t < (int)MU) ? load_u((uint32_t)t) : 0; };
+    // window R[0..MX] = limbs MU - MX .. MU of u 2^s (zeros below limb 0)
+    uint64_t R[MX + 1];
+    uint64_t below = raw((int)MU - MX - 1);   // raw limb under the window
+    {
+        uint64_t prev = below;
+#pragma unroll
+        for (int k = 0; k <= MX; k++) {
+            const uint64_t cur = raw((int)MU - MX + k);
+            R[k] = (cur << s) | ((prev >> 1) >> rs);
+            prev = cur;
+        }
+    }
+    const uint64_t d1 = D[MX - 1], d2 = D[MX - 2];
+    const uint64_t vr = recip_limb(d1);
+    int tn = (int)MU - MX - 1;   // shifted-dividend limb that enters the window next
+    for (int j = (int)MU - K; j >= 0; j--) {
+        const uint64_t u2 = R[MX], u1 = R[MX - 1], u0 = R[MX - 2];
+        uint64_t qh, rh;
+        bool rh_over = false;
+        if (u2 >= d1) {                        // u2 == d1: q-hat = B - 1, r-hat = u1 + d1
+            qh = ~0ull;
+            rh = u1 + d1;
+            rh_over = rh < u1;
+        } else {
+            qh = div_2by1(u2, u1, d1, vr, rh);
+        }
+        for (int t = 0; t < 2 && !rh_over; t++) {   // q-hat * d2 > r-hat * B + u0: one too large
+            const uint64_t p_lo = qh * d2, p_hi = __umul64hi(qh, d2);
+            if (p_hi > rh || (p_hi == rh && p_lo > u0)) {
+                qh -= 1;
+                const uint64_t nr = rh + d1;
+                rh_over = nr < rh;
+                rh = nr;
+            } else {
+                break;
+            }
+        }
+        // R -= q-hat * D
+        uint64_t carry = 0, borrow = 0;
+#pragma unroll
+        for (int k = 0; k < MX; k++) {
+            const uint64_t plo = qh * D[k], phi = __umul64hi(qh, D[k]);
+            const uint64_t sub = plo + carry;
+            carry = phi + (sub < plo ? 1 : 0);
+            const uint64_t y = R[k] - sub;
+            const uint64_t b1 = R[k] < sub ? 1 : 0;
+            R[k] = y - borrow;
+            borrow = b1 | (y < borrow ? 1 : 0);
+        }
+        {
+            const uint64_t y = R[MX] - carry;
+            const uint64_t b1 = R[MX] < carry ? 1 : 0;
+            R[MX] = y - borrow;
+            borrow = b1 | (y < borrow ? 1 : 0);
+        }
+        if (borrow) {                          // one too large after all: add D back
+            qh -= 1;
+            uint64_t c = 0;
+#pragma unroll
+            for (int k = 0; k < MX; k++) {
+                const uint64_t x = R[k] + D[k];
+                const uint64_t c1 = x < D[k] ? 1 : 0;
+                R[k] = x + c;
+                c = c1 | (R[k] < x ? 1 : 0);
+            }
+            R[MX] += c;
+        }
+        store_q((uint32_t)j, qh);
+        if (j > 0) {                           // slide the window down one limb
+#pragma unroll
+            for (int k = MX; k > 0; k--) R[k] = R[k - 1];
+            const uint64_t lower = raw(tn - 1);    // below = raw(tn)
+            R[0] = (below << s) | ((lower >> 1) >> rs);
+            below = lower;
+            tn--;
+        }
+    }
+    for (uint32_t i = (uint32_t)((int)MU - K + 1); i < MU; i++) store_q(i, 0);
+    // remainder: R[0..MX-1] = (r 2^s) B^zl
+    for (int z = 0; z < zl; z++) {
+#pragma unroll
+        for (int k = 0; k < MX - 1; k++) R[k] = R[k + 1];
+        R[MX - 1] = 0;
+    }
+#pragma unroll
+    for (int k = 0; k < MX; k++) {
+        const uint64_t hi = k + 1 < MX ? R[k + 1] : 0;
+        const uint64_t x = (R[k] >> s) | ((hi << 1) << rs);
+        if (k < (int)MV) store_r((uint32_t)k, x);
+    }
+    return 0;
+}
+
+// Borrow (or carry) into this lane of a warp-wide chain, from each lane's
+// generate g (out with nothing in) and propagate p (out only with one in):
+// bit l of (A + B) ^ A ^ B with A = ballot(g | p), B = ballot(g).  cout gets
+// the borrow out of lane 31.
+__device__ __forceinline__ uint64_t warp_chain_in(bool g, bool p, uint64_t& cout) {
+    const uint32_t A = __ballot_sync(0xffffffffu, g || p), Bm = __ballot_sync(0xffffffffu, g);
+    const uint64_t s = (uint64_t)A + Bm;
+    cout = s >> 32;
+    return ((s ^ A ^ Bm) >> (threadIdx.x & 31)) & 1u;
+}
+
+// One instance on one warp (all 32 lanes call with the same arguments): the
+// long division of div_thread with the divisor and the window spread over
+// the lanes, VPL limbs each (lane l holds positions l VPL .. l VPL + VPL - 1,
+// MX = 32 VPL), the top window limb R[MX] uniform in every lane.  Each
+// quotient limb costs the uniform 2-by-1 estimate, two in-lane borrow chains
+// (the high halves of q-hat D, then the low halves) resolved across lanes by
+// two ballots each, and a one-limb slide; the dividend streams in through a
+// 32-limb buffer loaded by the whole warp every 32 quotient limbs.
+template <int VPL, typename LoadU, typename LoadV, typename StoreQ, typename StoreR>
+__device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load_u, LoadV load_v, StoreQ store_q,
+                                            StoreR store_r) {
+    constexpr int MX = 32 * VPL;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31);
+    uint64_t D[VPL];
+#pragma unroll
+    for (int i = 0; i < VPL; i++) {
+        const int idx = lane * VPL + i - (MX - (int)MV);
+        D[i] = idx >= 0 ? load_v((uint32_t)idx) : 0;
+    }
+    int top_i = -1;
+#pragma unroll
+    for (int i = 0; i < VPL; i++)
+        if (D[i] != 0) top_i = i;
+    const uint32_t nz = __ballot_sync(FULL, top_i >= 0);
+    if (nz == 0) {
+        for (uint32_t i = lane; i < MU; i += 32) store_q(i, 0);
+        for (uint32_t i = lane; i < MV; i += 32) store_r(i, 0);
+        return 1;
+    }
+    const int tl = 31 - __clz((int)nz);
+    const int ptop = tl * VPL + __shfl_sync(FULL, top_i, tl);   // top nonzero position
+    const int K = ptop - (MX - (int)MV) + 1;
+    const int zl = MX - K;
+    for (int z = ptop; z < MX - 1; z++) {                      // one-limb shifts up
+        const uint64_t from_below = __shfl_up_sync(FULL, D[VPL - 1], 1);
+#pragma unroll
+        for (int i = VPL - 1; i > 0; i--) D[i] = D[i - 1];
+        D[0] = lane == 0 ? 0 : from_below;
+    }
+    const int s = __clzll((long long)__shfl_sync(FULL, D[VPL - 1], 31));
+    const int rs = 63 - s;   // x >> (64 - s) written as (x >> 1) >> rs: 0 when s == 0
+    {
+        const uint64_t below = __shfl_up_sync(FULL, D[VPL - 1], 1);
+        uint64_t prev = lane == 0 ? 0 : below;
+#pragma unroll
+        for (int i = 0; i < VPL; i++) {
+            const uint64_t cur = D[i];
+            D[i] = (cur << s) | ((prev >> 1) >> rs);
+            prev = cur;
+        }
+    }
+    const uint64_t d1 = __shfl_sync(FULL, D[VPL - 1], 31);
+    const uint64_t d2 = VPL >= 2 ? __shfl_sync(FULL, D[VPL >= 2 ? VPL - 2 : 0], 31) : __shfl_sync(FULL, D[0], 30);
+    const uint64_t vr = recip_limb(d1);
+
+    // the shifted dividend: sh(t) = limb t of u 2^s, t in [0, MU]
+    auto raw = [&](int t) -> uint64_t { return (t >= 0 && t < (int)MU) ? load_u((uint32_t)t) : 0; };
+    auto sh = [&](int t) -> uint64_t { return (raw(t) << s) | ((raw(t - 1) >> 1) >> rs); };
+    // window positions 0..MX-1 = limbs MU - MX .. MU - 1 of u 2^s, R[MX] = limb MU
+    uint64_t R[VPL];
+    {
+        const int t0 = (int)MU - MX + lane * VPL;
+        uint64_t prev = raw(t0 - 1);
+#pragma unroll
+        for (int i = 0; i < VPL; i++) {
+            const uint64_t cur = raw(t0 + i);
+            R[i] = (cur << s) | ((prev >> 1) >> rs);
+            prev = cur;
+        }
+    }
+    uint64_t rtop = (raw((int)MU - 1) >> 1) >> rs;
+    // stream buffer: lane l holds sh(base - l); limb c of it enters at the c-th slide
+    int base = (int)MU - MX - 1, c = 0;
+    uint64_t shb = sh(base - lane);
+    for (int j = (int)MU - K; j >= 0; j--) {
+        const uint64_t u2 = rtop;
+        const uint64_t u1 = __shfl_sync(FULL, R[VPL - 1], 31);
+        const uint64_t u0 = VPL >= 2 ? __shfl_sync(FULL, R[VPL >= 2 ? VPL - 2 : 0], 31) : __shfl_sync(FULL, R[0], 30);
+        uint64_t qh, rh;
+        bool rh_over = false;
+        if (u2 >= d1) {                        // u2 == d1: q-hat = B - 1, r-hat = u1 + d1
+            qh = ~0ull;
+            rh = u1 + d1;
+            rh_over = rh < u1;
+        } else {
+            qh = div_2by1(u2, u1, d1, vr, rh);
+        }
+        for (int t = 0; t < 2 && !rh_over; t++) {   // q-hat * d2 > r-hat * B + u0: one too large
+            const uint64_t p_lo = qh * d2, p_hi = __umul64hi(qh, d2);
+            if (p_hi > rh || (p_hi == rh && p_lo > u0)) {
+                qh -= 1;
+                const uint64_t nr = rh + d1;
+                rh_over = nr < rh;
+                rh = nr;
+            } else {
+                break;
+            }
+        }
+        // pass A: R -= (high halves of q-hat D) shifted up one position, in
+        // lane, borrows across lanes resolved by two ballots; the borrow into
+        // each lane is applied by pass B's chain
+        uint64_t coutA, coutB;
+        bool neg;
+        {
+            const uint64_t htop = __umul64hi(qh, D[VPL - 1]);
+            const uint64_t hb = __shfl_up_sync(FULL, htop, 1);
+            uint64_t Hs[VPL];
+            Hs[0] = lane == 0 ? 0 : hb;
+#pragma unroll
+            for (int i = 1; i < VPL; i++) Hs[i] = __umul64hi(qh, D[i - 1]);
+            const uint32_t gA = chain_sub<VPL>(R, Hs, 0);
+            bool zA = true;
+#pragma unroll
+            for (int i = 0; i < VPL; i++) zA &= R[i] == 0;
+            const uint32_t binA = (uint32_t)warp_chain_in(gA != 0, zA, coutA);
+            const uint64_t th = __shfl_sync(FULL, htop, 31);
+            const uint64_t x = rtop - th;
+            const bool bA = (rtop < th) || (x < coutA);
+            rtop = x - coutA;
+            // pass B: R -= low halves of q-hat D and the borrow from pass A;
+            // a lane of zeros that took A's borrow wrapped to all ones, which
+            // A's ballots already carried on, so it generates no B borrow
+            uint64_t Ls[VPL];
+#pragma unroll
+            for (int i = 0; i < VPL; i++) Ls[i] = qh * D[i];
+            const uint32_t gB = chain_sub<VPL>(R, Ls, binA) & (zA && binA ? 0u : 1u);
+            bool zB = true;
+#pragma unroll
+            for (int i = 0; i < VPL; i++) zB &= R[i] == 0;
+            uint32_t bin = (uint32_t)warp_chain_in(gB != 0, zB, coutB);
+            uint64_t Z[VPL];
+#pragma unroll
+            for (int i = 0; i < VPL; i++) Z[i] = 0;
+            chain_sub<VPL>(R, Z, bin);
+            const bool bB = rtop < coutB;
+            rtop -= coutB;
+            neg = bA || bB;                    // at most one of the two wraps
+        }
+        if (neg) {                             // one too large after all: add D back
+            qh -= 1;
+            uint64_t cy = 0;
+            bool allo = true;
+#pragma unroll
+            for (int i = 0; i < VPL; i++) {
+                const uint64_t x = R[i] + D[i];
+                const uint64_t c1 = x < D[i] ? 1 : 0;
+                const uint64_t y = x + cy;
+                cy = c1 | (y < x ? 1 : 0);
+                R[i] = y;
+                allo &= y == ~0ull;
+            }
+            uint64_t cout;
+            uint64_t cin = warp_chain_in(cy != 0, allo, cout);
+#pragma unroll
+            for (int i = 0; i < VPL; i++) {
+                const uint64_t y = R[i];
+                R[i] = y + cin;
+                cin &= y == ~0ull ? 1 : 0;
+            }
+            rtop += cout;
+        }
+        if (lane == 0) store_q((uint32_t)j, qh);
+        if (j > 0) {                           // slide the window down one limb
+            const uint64_t next = __shfl_sync(FULL, shb, c);
+            rtop = __shfl_sync(FULL, R[VPL - 1], 31);
+            const uint64_t from_below = __shfl_up_sync(FULL, R[VPL - 1], 1);
+#pragma unroll
+            for (int i = VPL - 1; i > 0; i--) R[i] = R[i - 1];
+            R[0] = lane == 0 ? next : from_below;
+            if (++c == 32) {
+                base -= 32;
+                c = 0;
+                shb = sh(base - lane);
+            }
+        }
+    }
+    for (uint32_t i = (uint32_t)((int)MU - K + 1) + lane; i < MU; i += 32) store_q(i, 0);
+    // remainder: positions 0..MX-1 hold (r 2^s) B^zl
+    for (int z = 0; z < zl; z++) {
+        const uint64_t from_above = __shfl_down_sync(FULL, R[0], 1);
+#pragma unroll
+        for (int i = 0; i < VPL - 1; i++) R[i] = R[i + 1];
+        R[VPL - 1] = lane == 31 ? 0 : from_above;
+    }
+    {
+        const uint64_t ab = __shfl_down_sync(FULL, R[0], 1);
+        const uint64_t above = lane == 31 ? 0 : ab;
+#pragma unroll
+        for (int i = 0; i < VPL; i++) {
+            const uint64_t hi = i + 1 < VPL ? R[i + 1 < VPL ? i + 1 : 0] : above;
+            const uint64_t x = (R[i] >> s) | ((hi << 1) << rs);
+            const int p = lane * VPL + i;
+            if (p < (int)MV) store_r((uint32_t)p, x);
+        }
+    }
+    return 0;
+}
+
+}  // namespace bi

@@ -17,7 +17,7 @@
 //     the 2-by-1 division by a precomputed reciprocal of Moller and Granlund
 //     ("Improved division by invariant integers", IEEE Trans. Computers
 //     60(2), 2011, Algorithm 4), on the u64 view of the instance.
-#include "divcore.cuh"   // recip_limb
+#include "divcore.cuh"   // recip_limb, div_2by1
 
 namespace bi {
 
@@ -136,29 +136,6 @@ __global__ void __launch_bounds__(PRIM_CTA) muld_kernel(const T* a, const T* dv,
 // quod: q = floor(a / d), rem = a mod d, d one limb per instance
 // (div.c quod, :165-181); d = 0 gives q = 0 and rem = 0.
 // ---------------------------------------------------------------------------
-// 2-by-1 division of (u1, u0) by a normalised d (top bit set), u1 < d, with
-// v = floor((B^2 - 1) / d) - B (Moller-Granlund Algorithm 4).
-__device__ __forceinline__ uint64_t div_2by1(uint64_t u1, uint64_t u0, uint64_t d, uint64_t v, uint64_t& r) {
-    // (q1, q0) = v * u1 + (u1, u0)
-    uint64_t q0 = v * u1;
-    uint64_t q1 = __umul64hi(v, u1);
-    const uint64_t s = q0 + u0;
-    q1 += u1 + (s < q0 ? 1 : 0);
-    q0 = s;
-    q1 += 1;
-    uint64_t rr = u0 - q1 * d;
-    if (rr > q0) {
-        q1 -= 1;
-        rr += d;
-    }
-    if (rr >= d) {
-        q1 += 1;
-        rr -= d;
-    }
-    r = rr;
-    return q1;
-}
-
 template <typename T>
 __device__ __forceinline__ uint64_t limb64_of(const T* x, uint32_t m, uint32_t i) {
     if constexpr (sizeof(T) == 8) {

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "divcore.cuh"
+#include "divsmall.cuh"
 #include "mulcore.cuh"
 #include "warpops.cuh"
 
@@ -42,6 +43,9 @@ constexpr int SERVE_CTA = 256;
 constexpr uint32_t SERVE_MAX_LIMBS = 2048;       // largest operand (64-bit limbs)
 constexpr uint64_t SERVE_WAIT_NS = 1000000000;   // give up on a slot after 1 s
 constexpr uint64_t SERVE_LOST = 0xFF;            // status of a request whose slot never filled
+// divisors up to this many limbs divide on warp 0 (long division), larger ones
+// on the whole CTA (shifted inverse): the single-request crossover
+constexpr uint32_t SERVE_DIV_WARP_MAX_MV = 128;
 
 struct alignas(64) ServeSlot {   // one request in the ring (mapped host memory)
     bi_desc d;                   // written first
@@ -233,12 +237,31 @@ __global__ void __launch_bounds__(SERVE_CTA, 2) serve_kernel(const ServeArgs A) 
                 };
                 mul_cta<MUL_C>(g, smem, scratch, lpdiv, load, store);
             } else {   // BI_OP_DIV (the host admits nothing else)
-                const DivGeom g = div_geom(d.m, d.mb, 8);
                 uint64_t* r2 = A.out + d.r2;
-                div_cta(
-                    g, smem, [&](uint32_t i) { return a[i]; }, [&](uint32_t i) { return b[i]; },
-                    [&](uint32_t i, uint64_t x) { r[i] = x; }, [&](uint32_t i, uint64_t x) { r2[i] = x; },
-                    [&](uint8_t code) { s_flag = code; });
+                auto ld_u = [&](uint32_t i) { return a[i]; };
+                auto ld_v = [&](uint32_t i) { return b[i]; };
+                auto st_q = [&](uint32_t i, uint64_t x) { r[i] = x; };
+                auto st_r = [&](uint32_t i, uint64_t x) { r2[i] = x; };
+                // long division on one thread or one warp where it finishes
+                // sooner than the CTA's shifted inverse (divsmall.cuh)
+                if (d.mb <= (uint32_t)DIV_THREAD_MAX_MV) {
+                    if (threadIdx.x == 0) {
+                        const uint8_t st = d.mb <= 4 ? div_thread<4>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
+                                                     : d.mb <= 8 ? div_thread<8>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
+                                                                 : div_thread<16>(d.m, d.mb, ld_u, ld_v, st_q, st_r);
+                        s_flag = st;
+                    }
+                } else if (d.mb <= SERVE_DIV_WARP_MAX_MV) {
+                    if (threadIdx.x < 32) {
+                        const uint8_t st = d.mb <= 32 ? div_warp<1>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
+                                                      : d.mb <= 64 ? div_warp<2>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
+                                                                   : div_warp<4>(d.m, d.mb, ld_u, ld_v, st_q, st_r);
+                        if (threadIdx.x == 0) s_flag = st;
+                    }
+                } else {
+                    const DivGeom g = div_geom(d.m, d.mb, 8);
+                    div_cta(g, smem, ld_u, ld_v, st_q, st_r, [&](uint8_t code) { s_flag = code; });
+                }
             }
         }
         __threadfence();

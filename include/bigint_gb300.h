@@ -126,6 +126,26 @@ bi_status bi_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t
 bi_status bi_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r,
                      uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
                      bi_stream stream);
+/* The method depends on the divisor's size in 64-bit limbs and on n (the */
+/* results do not: q and r are unique): schoolbook long division on one   */
+/* thread per instance up to 16 limbs and on one warp per instance up to  */
+/* 128 limbs, and up to 1024 limbs once n exceeds a few instances per SM; */
+/* otherwise the shifted inverse on one CTA per instance.  The _shinv     */
+/* entries take the shifted inverse at every size (the reference's        */
+/* algorithm), the _long entries long division (divisors up to 1024       */
+/* 64-bit limbs, else BI_EUNSUPPORTED); same arguments and results.       */
+bi_status bi_div_shinv_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r,
+                           uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
+                           bi_stream stream);
+bi_status bi_div_shinv_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r,
+                           uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
+                           bi_stream stream);
+bi_status bi_div_long_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r,
+                          uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
+                          bi_stream stream);
+bi_status bi_div_long_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t* r,
+                          uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
+                          bi_stream stream);
 
 /* ---------------------------------------------------------------------- */
 /* Host-pointer twins of the above (synchronous, pipelined; see top).     */

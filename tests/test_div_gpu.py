@@ -12,8 +12,8 @@ from bigint_gb300.workloads import splitmix64, uniform_limbs
 pytestmark = pytest.mark.gpu
 
 
-def _run(B, oracle, u, v):
-    q, r, st = B.div(B.to_device(u), B.to_device(v))
+def _run(B, oracle, u, v, method="auto"):
+    q, r, st = B.div(B.to_device(u), B.to_device(v), method=method)
     q, r, st = B.to_host(q, u.dtype), B.to_host(r, u.dtype), st.cpu().numpy()
     q_ref, r_ref, st_ref = oracle.div(u, v)
     assert (st == st_ref).all()
@@ -40,9 +40,10 @@ def test_reference_kats(bigint, golden):
         assert [int(x) for x in B.to_host(r, np.uint32)[0]] == k["r"], k["source"]
 
 
+@pytest.mark.parametrize("method", ["auto", "shinv", "long"])
 @pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
-@pytest.mark.parametrize("m", [1, 2, 3, 4, 5, 8, 13, 16, 31, 32, 33, 64, 100])
-def test_divisor_precision_sweep(bigint, oracle, dtype, m):
+@pytest.mark.parametrize("m", [1, 2, 3, 4, 5, 8, 13, 16, 17, 31, 32, 33, 64, 100])
+def test_divisor_precision_sweep(bigint, oracle, dtype, m, method):
     """Equal sizes, divisor precision 1..m as in prototypes/div.c:509-523."""
     n = 3 * m
     u = uniform_limbs(101 + m, n, m, dtype)
@@ -51,12 +52,13 @@ def test_divisor_precision_sweep(bigint, oracle, dtype, m):
         v[i, 1 + i % m:] = 0
         if v[i, 0] == 0:
             v[i, 0] = 1
-    _run(bigint, oracle, u, v)
+    _run(bigint, oracle, u, v, method)
 
 
+@pytest.mark.parametrize("method", ["auto", "shinv", "long"])
 @pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
 @pytest.mark.parametrize("mv", [1, 2, 7, 16, 50, 128, 512])
-def test_dividend_twice_divisor(bigint, oracle, dtype, mv):
+def test_dividend_twice_divisor(bigint, oracle, dtype, mv, method):
     """The uneven-batch division shape: dividend 2m limbs, divisor m limbs with a nonzero top limb."""
     n = max(4, min(64, 4000 // mv))
     u = uniform_limbs(201 + mv, n, 2 * mv, dtype)
@@ -71,7 +73,7 @@ def test_dividend_twice_divisor(bigint, oracle, dtype, mv):
     v[2] = 0
     v[2, 0] = 1
     v[2, -1] = 1                       # v = B^(m-1) + 1
-    _run(bigint, oracle, u, v)
+    _run(bigint, oracle, u, v, method)
 
 
 def test_special_values(bigint, oracle):
@@ -101,13 +103,69 @@ def test_zero_divisor_flagged(bigint, oracle):
     assert ei.value.status == 2
 
 
+@pytest.mark.parametrize("method", ["auto", "shinv", "long"])
 @pytest.mark.parametrize("mv", [256, 1024])
-def test_large_divisions(bigint, oracle, mv):
+def test_large_divisions(bigint, oracle, mv, method):
     n = 3
     u = uniform_limbs(301 + mv, n, 2 * mv)
     v = uniform_limbs(302 + mv, n, mv)
     v[:, -1] |= 1
-    _run(bigint, oracle, u, v)
+    _run(bigint, oracle, u, v, method)
+
+
+@pytest.mark.parametrize("mu,mv", [(16, 16), (17, 17), (40, 32), (40, 33), (2048, 1024), (2048, 1025), (2048, 2048)])
+def test_method_boundaries(bigint, oracle, mu, mv):
+    """Divisor sizes on either side of the long-division limits (16 and 1024
+    64-bit limbs) and the largest supported dividend, by both methods."""
+    n = 3
+    u = uniform_limbs(311 + mv, n, mu)
+    v = uniform_limbs(312 + mv, n, mv)
+    v[:, -1] |= 1
+    v[1, mv // 2:] = 0                 # shorter divisor in a wider row
+    v[1, mv // 2 - 1] |= 1
+    for method in ("auto", "shinv", "long"):
+        if method == "long" and mv > 1024:
+            with pytest.raises(bigint.BigIntError):
+                _run(bigint, oracle, u, v, method)
+        else:
+            _run(bigint, oracle, u, v, method)
+
+
+def _addback_rows(seed, mu, mv, n, bits):
+    """u = (qh v - 1) B^(mu - mv - 1) + low with v normalised: the quotient
+    estimate from the top limbs is qh, one more than the true top limb, so the
+    long division takes its add-back branch at the first quotient limb."""
+    import random
+    rng = random.Random(seed)
+    U, V = [], []
+    for _ in range(n):
+        v = rng.getrandbits(bits * mv) | (1 << (bits * mv - 1))
+        qh = rng.getrandbits(bits) | 1
+        extra = mu - mv - 1
+        u = ((qh * v - 1) << (bits * extra)) | rng.getrandbits(bits * extra) if extra else qh * v - 1
+        U.append(u)
+        V.append(v)
+    return U, V
+
+
+@pytest.mark.parametrize("method", ["auto", "shinv", "long"])
+@pytest.mark.parametrize("bits", [64, 32])
+@pytest.mark.parametrize("mu,mv", [(3, 2), (6, 5), (20, 16), (19, 18), (40, 31), (70, 64), (300, 200), (1500, 1024)])
+def test_add_back_cases(bigint, oracle, bits, mu, mv, method):
+    if bits == 32:
+        mu, mv = 2 * mu, 2 * mv
+    dtype = np.uint64 if bits == 64 else np.uint32
+    U, V = _addback_rows(1000 + mu + mv, mu, mv, 4, bits)
+    mask = (1 << bits) - 1
+    u = np.array([[(x >> (bits * i)) & mask for i in range(mu)] for x in U], dtype)
+    v = np.array([[(x >> (bits * i)) & mask for i in range(mv)] for x in V], dtype)
+    B = bigint
+    q, r, st = B.div(B.to_device(u), B.to_device(v), method=method)
+    q, r = B.to_host(q, dtype), B.to_host(r, dtype)
+    for i, (x, y) in enumerate(zip(U, V)):
+        assert sum(int(w) << (bits * k) for k, w in enumerate(q[i])) == x // y
+        assert sum(int(w) << (bits * k) for k, w in enumerate(r[i])) == x % y
+    assert (st.cpu().numpy() == 0).all()
 
 
 def test_host_entry(bigint, oracle):
