@@ -286,6 +286,26 @@ def run_reference(args) -> None:
 # GPU measurements
 # ---------------------------------------------------------------------------
 
+def div_method(mv: int, n: int, sms: int) -> str:
+    """The method bi_div_u64 picks for n divisions by mv-limb divisors
+    (div_use_long in divsmall.cuh): long division on one thread or one warp
+    per instance, or the shifted inverse on one CTA per instance."""
+    if mv <= 16:
+        return "long_thread"
+    if mv <= 128:
+        return "long_warp"
+    if mv <= 1024 and n > (2 if mv <= 256 else 3 if mv <= 512 else 6) * sms:
+        return "long_warp"
+    return "shinv"
+
+
+def long_div_limb_products(mu: int, mv: int) -> int:
+    """64x64-bit limb products of schoolbook long division of a mu-limb
+    dividend by an mv-limb divisor with a nonzero top limb: one q-hat * v row
+    per quotient limb (the estimates' own products are not counted)."""
+    return (mu - mv + 1) * mv
+
+
 def div_limb_products(mu: int, mv: int) -> int:
     """64x64-bit limb products in the multiplications one division performs
     (the shifted-inverse division of divcore.cuh on a mu-limb dividend and an
@@ -378,10 +398,16 @@ def measure_extra(B, L, stream, args):
         st = torch.empty(n, dtype=torch.uint8, device="cuda")
         ms = event_time(stream, lambda: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
                                                                st.data_ptr(), 2 * mv, mv, n, sp)), 3, 1)
-        wp = 4 * div_limb_products(2 * mv, mv)   # 32x32-bit word products per division
-        div[f"m{mv}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4),
+        ms_shinv = event_time(stream, lambda: check(L, L.bi_div_shinv_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(),
+                                                                           rr.data_ptr(), st.data_ptr(), 2 * mv, mv, n,
+                                                                           sp)), 3, 1)
+        method = div_method(mv, n, torch.cuda.get_device_properties(0).multi_processor_count)
+        # 32x32-bit word products per division of the method that ran
+        wp = 4 * (div_limb_products(2 * mv, mv) if method == "shinv" else long_div_limb_products(2 * mv, mv))
+        div[f"m{mv}_n{n}"] = {"method": method, "instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4),
                               "word_products_per_div": wp, "word_products_per_s": wp * n / ms * 1e3,
-                              "frac_of_intpipe_peak": round(wp * n / ms * 1e3 / peak_wps, 4)}
+                              "frac_of_intpipe_peak": round(wp * n / ms * 1e3 / peak_wps, 4),
+                              "shinv_instances_per_s": round(n / ms_shinv * 1e3)}
         del u, v, q, rr, st
     out["div_u64_2m_by_m"] = div
     out["uneven_batch"] = measure_uneven_batch(B, L, stream)
@@ -671,9 +697,11 @@ def run_single(args) -> None:
         v[:, -1] |= 1
         q, rr = torch.empty_like(u), torch.empty_like(v)
         st = torch.empty(n, dtype=torch.uint8, device="cuda")
-        ms = event_time(stream, lambda: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
-                                                               st.data_ptr(), 2 * mv, mv, n, sp)), args.steps, args.warmup)
-        print(json.dumps({"workload": w, "m": mv, "n": n, "ms": ms, "instances_per_s": n / ms * 1e3}))
+        fn = L.bi_div_u64 if args.div_method == "auto" else getattr(L, f"bi_div_{args.div_method}_u64")
+        ms = event_time(stream, lambda: check(L, fn(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
+                                                    st.data_ptr(), 2 * mv, mv, n, sp)), args.steps, args.warmup)
+        print(json.dumps({"workload": w, "m": mv, "n": n, "method": args.div_method, "ms": ms,
+                          "instances_per_s": n / ms * 1e3}))
     elif w == "batch":
         d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=args.batch_n)
         din = B.to_device(arena)
@@ -862,6 +890,7 @@ def main():
     ap.add_argument("--total-limbs-log2", type=int, default=27)
     ap.add_argument("--mul-m", type=int, default=1024)
     ap.add_argument("--div-m", type=int, default=256)
+    ap.add_argument("--div-method", default="auto", choices=["auto", "shinv", "long"])
     ap.add_argument("--batch-n", type=int, default=100_000)
     ap.add_argument("--serve-rate", type=int, default=0, help="serve workload: one offered load (requests/s)")
     ap.add_argument("--no-extras", action="store_true")

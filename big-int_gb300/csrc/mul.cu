@@ -129,26 +129,33 @@ mulchain_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict_
 }
 
 // ---------------------------------------------------------------------------
-// Warp-level full product for small operands: G lanes per instance (G = the
-// power of two >= L, several instances per warp when L < 32; written for
-// P = Lpad / G column pairs per lane, which also covers L up to 128 with
-// G = 32), no CTA barrier.  The library routes full products of
-// L <= MUL_WARP_MAX_L = 32 here: faster than the CTA kernel at L = 32
-// (2048 bits), slower at L = 64, where each lane's column loop costs more
-// instructions per word product than the CTA kernel's row windows.  Operands padded to Lpad = G*P limbs sit in the
-// warp's shared memory; lane t of an instance accumulates the product
-// columns t + G*j, j < 2P, as 3-word sums (mul.lo/hi + add.cc chain),
-// pairing low column j with high column 2P-1-j so every lane does
-// G(2j+1) terms in phase j.  The column sums s_c = c0 + c1 B + c2 B^2 are
-// folded into limbs by two additions row by row (c0 + c1 shifted one column,
-// then + c2 shifted two), carries resolved with ballots within the instance.
+// Warp-level full product for small operands, on 32-bit words: G lanes per
+// instance (several instances per warp when G < 32), operands padded to
+// M = 2G words in the warp's shared memory (b twice over, so that
+// b[(c - i) mod M] is at a compile-time offset from a per-lane base), no
+// CTA barrier.  The library routes full products of at most 64 32-bit words
+// (32 64-bit limbs) here, for both limb types.
+//
+// Lane t accumulates four product columns as 3-word sums: 2t and 2t + M
+// (pair A: term a_i b_((2t - i) mod M) belongs to column 2t for i <= 2t and
+// to column 2t + M above) and 2t + 1, 2t + 1 + M (pair B, likewise) -- M
+// terms a pair, the same in every lane.  A term is three instructions,
+// mad.lo.cc / madc.hi.cc / addc on the integer multiply-add pipe with the
+// carry flag; each pair runs one accumulator over all M terms and a snapshot
+// at i = 2t (2t + 1) splits it into the low column (the snapshot) and the
+// high one (the rest).  Operands come two words a load: a_i, a_(i+1) are
+// one broadcast 64-bit load, and b's two words for pairs A and B are one
+// 64-bit load at the lane's base.  The columns then fold into 64-bit limbs:
+// lane t's columns 2t and 2t + 1 make the value v0 + v1 B at limb t
+// (B = 2^64, v1 < 2^39), likewise at limb t + G, and limb p of the product
+// is v0_p + v1_(p-1) with the carries resolved by ballots in the instance.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void mac3(uint64_t& c0, uint64_t& c1, uint64_t& c2, uint64_t x, uint64_t y) {
-    asm("{\n\t.reg .u64 lo, hi;\n\t"
-        "mul.lo.u64 lo, %3, %4;\n\tmul.hi.u64 hi, %3, %4;\n\t"
-        "add.cc.u64 %0, %0, lo;\n\taddc.cc.u64 %1, %1, hi;\n\taddc.u64 %2, %2, 0;\n\t}"
-        : "+l"(c0), "+l"(c1), "+l"(c2)
-        : "l"(x), "l"(y));
+
+// (c0, c1, c2) += x * y over 32-bit words, carries in the condition code
+__device__ __forceinline__ void mac3w(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t x, uint32_t y) {
+    asm("mad.lo.cc.u32 %0, %3, %4, %0;\n\tmadc.hi.cc.u32 %1, %3, %4, %1;\n\taddc.u32 %2, %2, 0;"
+        : "+r"(c0), "+r"(c1), "+r"(c2)
+        : "r"(x), "r"(y));
 }
 
 // carry into lane t of a G-lane group (lanes base..base+G-1) for per-lane
@@ -163,123 +170,138 @@ __device__ __forceinline__ uint32_t group_carry(uint32_t g, uint32_t p, uint32_t
     return (uint32_t)((s ^ A ^ B) >> t) & 1u;
 }
 
-template <typename T, int P, int G>
-__global__ void __launch_bounds__(256)
-mul_warp_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, uint64_t n, uint32_t m,
-                uint32_t L) {
-    extern __shared__ __align__(16) uint64_t smem[];
+// Small CTAs (4 warps): a batch that fills one wave spreads within a warp or
+// so of evenly over the SMs.
+constexpr int MUL_WARP_CTA = 128;
+
+// word x (32-bit) of operand row p with `words` words
+template <typename T>
+__device__ __forceinline__ uint32_t word32(const T* p, uint32_t words, uint32_t x) {
+    if (x >= words) return 0;
+    if constexpr (sizeof(T) == 8) return (uint32_t)(p[x >> 1] >> (32 * (x & 1)));
+    else return p[x];
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__(MUL_WARP_CTA)
+mul_warp_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, uint64_t n, uint32_t m) {
+    constexpr uint32_t M = 2 * G;                      // padded words per operand
+    constexpr uint32_t ipw = 32 / G;                   // instances per warp
+    extern __shared__ __align__(16) uint32_t smw[];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t Lpad = G * P;
-    const uint32_t ipw = 32 / G;                       // instances per warp
     const uint32_t lg = lane / G, t = lane - lg * G;   // instance within the warp, lane within it
     const uint32_t base = lg * G;
-    uint64_t* sa = smem + ((size_t)warp * ipw + lg) * 2 * Lpad;
-    uint64_t* sb = sa + Lpad;
-    const uint32_t out_limbs = 2 * L;
+    uint32_t* sa = smw + ((size_t)warp * ipw + lg) * 3 * M;   // a: M words, then b twice: 2M words
+    uint32_t* sb = sa + M;
+    const uint32_t words = sizeof(T) == 8 ? 2 * m : m;        // operand words
+    const uint32_t out_words = 2 * words;
     const uint64_t nwarps = (uint64_t)gridDim.x * (blockDim.x >> 5);
     for (uint64_t wi = (uint64_t)blockIdx.x * (blockDim.x >> 5) + warp; wi * ipw < n; wi += nwarps) {
         const uint64_t inst = wi * ipw + lg;
         const bool valid = inst < n;
-        for (uint32_t x = t; x < Lpad; x += G) {
-            uint64_t va = 0, vb = 0;
-            if (valid && x < L) {
-                if constexpr (sizeof(T) == 8) {
-                    va = a[inst * m + x];
-                    vb = b[inst * m + x];
-                } else {
-                    const uint64_t w0 = inst * m + 2 * x;
-                    va = a[w0];
-                    vb = b[w0];
-                    if (2 * x + 1 < m) {
-                        va |= (uint64_t)a[w0 + 1] << 32;
-                        vb |= (uint64_t)b[w0 + 1] << 32;
-                    }
-                }
-            }
-            sa[x] = va;
-            sb[x] = vb;
+        {
+            const T* pa = a + inst * m;
+            const T* pb = b + inst * m;
+            const uint32_t x0 = 2 * t, x1 = 2 * t + 1;
+            const uint32_t a0 = valid ? word32(pa, words, x0) : 0, a1 = valid ? word32(pa, words, x1) : 0;
+            const uint32_t b0 = valid ? word32(pb, words, x0) : 0, b1 = valid ? word32(pb, words, x1) : 0;
+            sa[x0] = a0;
+            sa[x1] = a1;
+            sb[x0] = b0;
+            sb[x1] = b1;
+            sb[x0 + M] = b0;
+            sb[x1 + M] = b1;
         }
         __syncwarp();
-        uint64_t acc[2 * P][3];
+        uint32_t A0 = 0, A1 = 0, A2 = 0, B0 = 0, B1 = 0, B2 = 0;
+        uint32_t SA0 = 0, SA1 = 0, SA2 = 0, SB0 = 0, SB1 = 0, SB2 = 0;
+        // pair A reads b[(2t - i) mod M] = sb[M + 2t - i], pair B the word above
+        const uint32_t* bp = sb + M + 2 * t;
 #pragma unroll
-        for (int j = 0; j < P; j++) {
-            const uint32_t lo = t + G * j;                  // a low column ...
-            const uint32_t hi = t + G * (2 * P - 1 - j);    // ... and its high partner (>= Lpad)
-            const uint32_t hi_i0 = hi - Lpad + 1;           // first row of the high column
-            const uint32_t len = G * (2 * j + 1);           // terms of both, the same in every lane
-            uint64_t c0 = 0, c1 = 0, c2 = 0;
-#pragma unroll
-            for (uint32_t rr = 0; rr < len; rr++) {
-                const bool low = rr <= lo;
-                const uint32_t i = low ? rr : hi_i0 + (rr - lo - 1);
-                const uint32_t col = low ? lo : hi;
-                mac3(c0, c1, c2, sa[i], sb[col - i]);
-                if (rr == lo) {
-                    acc[j][0] = c0; acc[j][1] = c1; acc[j][2] = c2;
-                    c0 = c1 = c2 = 0;
-                }
-            }
-            acc[2 * P - 1 - j][0] = c0; acc[2 * P - 1 - j][1] = c1; acc[2 * P - 1 - j][2] = c2;
+        for (int k = 0; k < (int)G; k++) {
+            const int i = 2 * k;
+            const uint2 av = *reinterpret_cast<const uint2*>(sa + i);        // a_i, a_(i+1)
+            const uint2 bv = *reinterpret_cast<const uint2*>(bp - i);        // b for A at i, b for B at i
+            // i: A takes b[2t - i], B takes b[2t + 1 - i]
+            mac3w(A0, A1, A2, av.x, bv.x);
+            mac3w(B0, B1, B2, av.x, bv.y);
+            const bool snap = k == (int)t;
+            if (snap) { SA0 = A0; SA1 = A1; SA2 = A2; }
+            // i + 1: A takes b[2t - i - 1], B takes b[2t - i] (= bv.x)
+            const uint32_t bA1 = bp[-i - 1];
+            mac3w(A0, A1, A2, av.y, bA1);
+            mac3w(B0, B1, B2, av.y, bv.x);
+            if (snap) { SB0 = B0; SB1 = B1; SB2 = B2; }
         }
         __syncwarp();   // the shared operands are rewritten by the next round
-        // fold: row jj holds columns G*jj + t
-        uint32_t cy1 = 0, cy2 = 0;                  // carries between rows (both additions)
-        uint64_t prev1 = 0, prev2a = 0, prev2b = 0;  // c1 of column G*jj-1; c2 of columns G*jj-2, G*jj-1
+        // high columns: the rest after the snapshots
+        uint32_t HA0, HA1, HA2, HB0, HB1, HB2;
+        asm("sub.cc.u32 %0, %3, %6;\n\tsubc.cc.u32 %1, %4, %7;\n\tsubc.u32 %2, %5, %8;"
+            : "=r"(HA0), "=r"(HA1), "=r"(HA2)
+            : "r"(A0), "r"(A1), "r"(A2), "r"(SA0), "r"(SA1), "r"(SA2));
+        asm("sub.cc.u32 %0, %3, %6;\n\tsubc.cc.u32 %1, %4, %7;\n\tsubc.u32 %2, %5, %8;"
+            : "=r"(HB0), "=r"(HB1), "=r"(HB2)
+            : "r"(B0), "r"(B1), "r"(B2), "r"(SB0), "r"(SB1), "r"(SB2));
+        // limb value v0 + v1 B from columns (x0, x1, x2) and (y0, y1, y2) one word apart
+        auto limb = [](uint32_t x0, uint32_t x1, uint32_t x2, uint32_t y0, uint32_t y1, uint32_t y2, uint64_t& v1) {
+            const uint64_t lo = ((uint64_t)x1 << 32) | x0;
+            const uint64_t add = (uint64_t)y0 << 32;
+            const uint64_t v0 = lo + add;
+            v1 = (uint64_t)x2 + (((uint64_t)y2 << 32) | y1) + (v0 < add ? 1 : 0);
+            return v0;
+        };
+        uint64_t v1r[2], v0r[2];
+        v0r[0] = limb(SA0, SA1, SA2, SB0, SB1, SB2, v1r[0]);
+        v0r[1] = limb(HA0, HA1, HA2, HB0, HB1, HB2, v1r[1]);
+        // fold: row jj holds limb G jj + t
+        uint32_t cy = 0;
+        uint64_t prev = 0;   // v1 of the limb below this row's first
 #pragma unroll
-        for (int jj = 0; jj < 2 * P; jj++) {
-            // c1 of column c-1 and c2 of column c-2
-            uint64_t s1 = __shfl_up_sync(0xffffffffu, acc[jj][1], 1, G);
-            if (t == 0) s1 = prev1;
-            uint64_t s2 = __shfl_up_sync(0xffffffffu, acc[jj][2], 2, G);
-            if (t == 0) s2 = prev2a;
-            else if (t == 1) s2 = prev2b;
-            prev1 = __shfl_sync(0xffffffffu, acc[jj][1], base + G - 1);
-            prev2a = __shfl_sync(0xffffffffu, acc[jj][2], base + G - 2);
-            prev2b = __shfl_sync(0xffffffffu, acc[jj][2], base + G - 1);
-            // y = c0 + s1
-            const uint64_t y = acc[jj][0] + s1;
+        for (int jj = 0; jj < 2; jj++) {
+            uint64_t s1 = __shfl_up_sync(0xffffffffu, v1r[jj], 1, G);
+            if (t == 0) s1 = prev;
+            prev = __shfl_sync(0xffffffffu, v1r[jj], base + G - 1);
+            const uint64_t y = v0r[jj] + s1;
             uint32_t co;
-            const uint32_t k1 = group_carry(y < s1, y == ~0ull, cy1, G, base, t, co);
-            cy1 = co;
-            const uint64_t y2 = y + k1;
-            // v = y2 + s2
-            const uint64_t v = y2 + s2;
-            const uint32_t k2 = group_carry(v < s2, v == ~0ull, cy2, G, base, t, co);
-            cy2 = co;
-            const uint32_t c = G * jj + t;
-            if (valid && c < out_limbs) {
-                const uint64_t out = v + k2;
+            const uint32_t k1 = group_carry(y < s1, y == ~0ull, cy, G, base, t, co);
+            cy = co;
+            const uint64_t out = y + k1;
+            const uint32_t c = G * jj + t;   // 64-bit limb of the product
+            if (valid) {
                 if constexpr (sizeof(T) == 8) {
-                    r[inst * out_limbs + c] = out;
+                    if (c < m * 2) r[inst * (2ull * m) + c] = out;
                 } else {
                     const uint64_t w0 = inst * (2ull * m) + 2 * c;
-                    if (2 * c < 2 * m) r[w0] = (uint32_t)out;
-                    if (2 * c + 1 < 2 * m) r[w0 + 1] = (uint32_t)(out >> 32);
+                    if (2 * c < out_words) r[w0] = (uint32_t)out;
+                    if (2 * c + 1 < out_words) r[w0 + 1] = (uint32_t)(out >> 32);
                 }
             }
         }
     }
 }
 
-template <typename T, int P, int G>
-static bi_status mul_warp_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, uint32_t L, cudaStream_t st) {
+template <typename T, int G>
+static bi_status mul_warp_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     constexpr uint32_t ipw = 32 / G;
+    constexpr uint32_t WPB = MUL_WARP_CTA / 32;   // warps per CTA
     const uint64_t warps = (n + ipw - 1) / ipw;
-    const uint64_t blocks = (warps + 7) / 8;
-    const uint64_t cap = (uint64_t)num_sms() * 32;
-    const size_t smem = (size_t)8 * ipw * 2 * G * P * 8;
-    mul_warp_kernel<T, P, G><<<(unsigned)(blocks < cap ? blocks : cap), 256, smem, st>>>(a, b, r, n, m, L);
+    const uint64_t blocks = (warps + WPB - 1) / WPB;
+    const uint64_t cap = (uint64_t)num_sms() * 64;
+    const size_t smem = (size_t)WPB * ipw * 3 * (2 * G) * 4;
+    mul_warp_kernel<T, G><<<(unsigned)(blocks < cap ? blocks : cap), MUL_WARP_CTA, smem, st>>>(a, b, r, n, m);
     return check_launch("mulfull warp kernel");
 }
 
-// Full products of u64-view size L <= MUL_WARP_MAX_L go to the warp kernel.
+// Full products of at most 64 32-bit words per operand go to the warp kernel;
+// G = the power of two >= half the operand's words.
 template <typename T>
-static bi_status mul_warp(const T* a, const T* b, T* r, uint32_t m, uint64_t n, uint32_t L, cudaStream_t st) {
-    if (L <= 2) return mul_warp_launch<T, 1, 2>(a, b, r, m, n, L, st);
-    if (L <= 4) return mul_warp_launch<T, 1, 4>(a, b, r, m, n, L, st);
-    if (L <= 8) return mul_warp_launch<T, 1, 8>(a, b, r, m, n, L, st);
-    if (L <= 16) return mul_warp_launch<T, 1, 16>(a, b, r, m, n, L, st);
-    return mul_warp_launch<T, 1, 32>(a, b, r, m, n, L, st);
+static bi_status mul_warp(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
+    const uint32_t half = sizeof(T) == 8 ? m : (m + 1) / 2;
+    if (half <= 2) return mul_warp_launch<T, 2>(a, b, r, m, n, st);
+    if (half <= 4) return mul_warp_launch<T, 4>(a, b, r, m, n, st);
+    if (half <= 8) return mul_warp_launch<T, 8>(a, b, r, m, n, st);
+    if (half <= 16) return mul_warp_launch<T, 16>(a, b, r, m, n, st);
+    return mul_warp_launch<T, 32>(a, b, r, m, n, st);
 }
 
 // ---------------------------------------------------------------------------
@@ -292,7 +314,7 @@ static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n
     constexpr int C = MUL_C;
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
-    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, L, st);
+    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, st);
     // at least two CTAs per SM when the batch is small: fewer instances per CTA
     const uint64_t fill = (n + 2ull * num_sms() - 1) / (2ull * num_sms());
     MulGeom g = mul_geometry(L, FULL, fill < 256 ? (uint32_t)(fill ? fill : 1) : 256u);
