@@ -28,7 +28,7 @@ Multi-GPU: instances are independent, so N ranks run N replicas of the step
 (weak scaling, no collective on the data path; NCCL only carries the barrier
 and the max over ranks of the elapsed time).
 
-`--workload add|sub|mul|div|batch` with `--bits`, `--total-limbs-log2`,
+`--workload add|sub|mul|mul2048|div|batch|serve` with `--bits`, `--total-limbs-log2`,
 `--mul-m`, `--div-m`, `--batch-n` runs one operation on one size, or the
 uneven batch, alone (used for profiling).
 """
@@ -702,6 +702,18 @@ def run_single(args) -> None:
                                                     st.data_ptr(), 2 * mv, mv, n, sp)), args.steps, args.warmup)
         print(json.dumps({"workload": w, "m": mv, "n": n, "method": args.div_method, "ms": ms,
                           "instances_per_s": n / ms * 1e3}))
+    elif w == "mul2048":
+        from bigint_gb300.workloads import mul2048_u32
+
+        a, b = mul2048_u32()
+        da, db = B.to_device(a), B.to_device(b)
+        r = torch.empty((a.shape[0], 128), dtype=torch.int32, device="cuda")
+        n = a.shape[0]
+        ms = graph_time(lambda st: check(L, L.bi_mulfull_u32(da.data_ptr(), db.data_ptr(), r.data_ptr(), 64, n, st)))
+        x = torch.zeros(2, dtype=torch.int64, device="cuda")
+        ms0 = graph_time(lambda st: check(L, L.bi_add_u64(x.data_ptr(), x.data_ptr(), x.data_ptr(), 1, 1, st)))
+        print(json.dumps({"workload": w, "n": n, "ms": ms, "instances_per_s": n / ms * 1e3,
+                          "one_limb_add_ms": ms0, "timing": "one replay of a CUDA graph of 20 launches"}))
     elif w == "batch":
         d, arena, out_limbs, nflags = B.workloads.uneven_batch(n=args.batch_n)
         din = B.to_device(arena)
@@ -885,7 +897,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="addsub", choices=["addsub", "add", "sub", "mul", "div", "batch", "serve"])
+    ap.add_argument("--workload", default="addsub",
+                    choices=["addsub", "add", "sub", "mul", "mul2048", "div", "batch", "serve"])
     ap.add_argument("--bits", type=int, default=0, help="restrict the add/sub sweep to one size")
     ap.add_argument("--total-limbs-log2", type=int, default=27)
     ap.add_argument("--mul-m", type=int, default=1024)
