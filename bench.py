@@ -360,9 +360,19 @@ def measure_extra(B, L, stream, args):
         rt = torch.empty((n, m), dtype=torch.int64, device="cuda")
         ms_t = event_time(stream, lambda: check(L, L.bi_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, sp)), 5)
         wp = n * (2 * m) ** 2
+        # the same calls after the autotuner picked the tiling on these operands
+        chosen = (ctypes.c_int * 2)()
+        check(L, L.bi_mul_autotune_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, 1, 3,
+                                       ctypes.cast(chosen, ctypes.c_void_p), sp))
+        ms_tuned = event_time(stream, lambda: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n,
+                                                                         sp)), 5)
+        check(L, L.bi_mul_set_tuning_u64(m, 1, 0, 0))       # back to the library's own choice
         mul[f"m{m}_n{n}"] = {"full_instances_per_s": round(n / ms * 1e3), "full_ms": round(ms, 4),
                              "word_products_per_s": wp / ms * 1e3, "frac_of_intpipe_peak": round(wp / ms * 1e3 / peak_wps, 4),
-                             "truncated_instances_per_s": round(n / ms_t * 1e3), "truncated_ms": round(ms_t, 4)}
+                             "truncated_instances_per_s": round(n / ms_t * 1e3), "truncated_ms": round(ms_t, 4),
+                             "autotuned_full_instances_per_s": round(n / ms_tuned * 1e3),
+                             "autotuned_frac_of_intpipe_peak": round(wp / ms_tuned * 1e3 / peak_wps, 4),
+                             "autotuned_tiling": {"instances_per_cta": chosen[0], "row_slices": chosen[1]}}
         del a, b, r, rt
     out["mul_u64_full"] = mul
     a, b = mul2048_u32()

@@ -97,6 +97,10 @@ SIGNATURES: dict[str, list] = {
     "bi_max_limbs_mul_u32": [],
     "bi_div_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
     "bi_div_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
+    "bi_mul_autotune_u64": [_P, _P, _P, _U32, _U64, _I, _I, _P, _P],
+    "bi_mul_autotune_u32": [_P, _P, _P, _U32, _U64, _I, _I, _P, _P],
+    "bi_mul_set_tuning_u64": [_U32, _I, _I, _I],
+    "bi_mul_set_tuning_u32": [_U32, _I, _I, _I],
     "bi_div_shinv_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
     "bi_div_shinv_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
     "bi_div_long_u64": [_P, _P, _P, _P, _P, _U32, _U32, _U64, _P],
@@ -279,6 +283,30 @@ def div(u, v, q=None, r=None, status=None, stream=None, method="auto"):
     _check(getattr(lib(), name)(u.data_ptr(), v.data_ptr(), q.data_ptr(), r.data_ptr(),
                                 status.data_ptr(), mu, mv, n, _stream_ptr(stream)))
     return q, r, status
+
+
+def mul_autotune(a, b, r=None, full: bool = True, reps: int = 3, stream=None):
+    """Time the CTA multiply's tilings on (a, b), keep the fastest for this
+    (limb width, full, m); returns (instances per CTA, slices), (0, 0) where
+    the warp kernel runs.  r receives the product as mulfull/mul write it."""
+    import torch
+
+    _dev2d(a, "a"), _dev2d(b, "b")
+    n, m = a.shape
+    if r is None:
+        r = torch.empty((n, 2 * m if full else m), dtype=a.dtype, device=a.device)
+    chosen = (ctypes.c_int * 2)()
+    _check(getattr(lib(), f"bi_mul_autotune_{_wsuffix(a)}")(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n,
+                                                           1 if full else 0, reps, ctypes.cast(chosen, ctypes.c_void_p),
+                                                           _stream_ptr(stream)))
+    return int(chosen[0]), int(chosen[1])
+
+
+def mul_set_tuning(m: int, dtype, full: bool, ipc: int, slices: int = 1):
+    """Set the CTA multiply's tiling for (limb width, full, m) by hand; ipc=0
+    returns to the library's own choice."""
+    w = "u64" if np.dtype(dtype).itemsize == 8 else "u32"
+    _check(getattr(lib(), f"bi_mul_set_tuning_{w}")(m, 1 if full else 0, ipc, slices))
 
 
 def add_chain(a, b, p: int, out=None, stream=None):

@@ -6,6 +6,8 @@
 #include <type_traits>
 
 #include "blockops.cuh"
+#include "divlimb.cuh"
+#include "divsmall.cuh"
 
 namespace bi {
 
@@ -21,163 +23,10 @@ struct DivGeom {
     uint32_t smem_limbs;
 };
 
-// floor((2^128 - 1) / d) - 2^64 for d >= 2^63: the low limb of a one-limb
-// reciprocal (the quotient is in (2^64, 2^65)), in integer arithmetic apart
-// from the seed.  Seed: the correctly rounded single-precision reciprocal of
-// the top 24 bits of d (relative error below 2^-22, so v is off by less than
-// 2^43).  Two Newton steps Y <- Y + Y r / 2^128 on Y = 2^64 + v, with
-// r = r(v) = (B - d) B - 1 - v d the exact residual (a signed 128-bit value),
-// take the error to a few units; comparing r(v) with 0 and d then fixes v to
-// the exact floor (at most two unit steps over 220,000 checked divisors,
-// including 2^63, 2^64 - 1 and every divisor with a one-bit tail).
-__device__ __forceinline__ void recip_residual(uint64_t d, uint64_t v, int64_t& r_hi, uint64_t& r_lo) {
-    const uint64_t a_hi = (0 - d) - 1, a_lo = ~0ull;   // (B - d) B - 1
-    const uint64_t p_lo = v * d, p_hi = __umul64hi(v, d);
-    r_lo = a_lo - p_lo;
-    r_hi = (int64_t)(a_hi - p_hi - (a_lo < p_lo ? 1 : 0));
-}
-
-// One Newton step: Y r / 2^128 = r_hi + v r_hi / 2^64 + (a part below 2),
-// added to v with saturation to [0, 2^64 - 1], where the answer lies.
-__device__ __forceinline__ uint64_t recip_newton(uint64_t d, uint64_t v) {
-    int64_t r_hi;
-    uint64_t r_lo;
-    recip_residual(d, v, r_hi, r_lo);
-    if (r_hi >= 0) {
-        const uint64_t m = (uint64_t)r_hi;
-        const uint64_t hi = __umul64hi(v, m);
-        const uint64_t delta = m + hi;                 // < 2^44: no wrap
-        return v + delta < v ? ~0ull : v + delta;
-    }
-    const uint64_t m = (uint64_t)(-r_hi);
-    const uint64_t delta = m + __umul64hi(v, m);
-    return delta > v ? 0ull : v - delta;
-}
-
-__device__ __forceinline__ uint64_t recip_limb(uint64_t d) {
-    // seed: 1 / f for f = the top 24 bits of d, f in [2^23, 2^24) exactly
-    // representable; the reciprocal lies in (2^-24, 2^-23]
-    const float rf = __frcp_rn(__uint2float_rn((uint32_t)(d >> 40)));
-    const uint32_t bits = __float_as_uint(rf);
-    // (1 + frac 2^-23) 2^-24 * 2^88 = 2^64 + frac 2^41; 2^-23 only for f = 2^23
-    uint64_t v = ((bits >> 23) & 0xffu) == 127u - 23u ? ~0ull : (uint64_t)(bits & 0x7fffffu) << 41;
-    v = recip_newton(d, v);
-    v = recip_newton(d, v);
-    int64_t r_hi;
-    uint64_t r_lo;
-    for (int it = 0; it < 8; it++) {   // at most two steps
-        recip_residual(d, v, r_hi, r_lo);
-        if (r_hi < 0 && v > 0) { v -= 1; continue; }
-        if ((r_hi > 0 || r_lo >= d) && v < ~0ull) { v += 1; continue; }
-        break;
-    }
-    return v;
-}
-
-// 2-by-1 division of (u1, u0) by a normalised d (top bit set), u1 < d, with
-// its reciprocal v = recip_limb(d) (Moller and Granlund, "Improved division
-// by invariant integers", IEEE Trans. Computers 60(2), 2011, Algorithm 4).
-__device__ __forceinline__ uint64_t div_2by1(uint64_t u1, uint64_t u0, uint64_t d, uint64_t v, uint64_t& r) {
-    uint64_t q0 = v * u1;
-    uint64_t q1 = __umul64hi(v, u1);
-    const uint64_t s = q0 + u0;
-    q1 += u1 + (s < q0 ? 1 : 0);
-    q0 = s;
-    q1 += 1;
-    uint64_t rr = u0 - q1 * d;
-    if (rr > q0) {
-        q1 -= 1;
-        rr += d;
-    }
-    if (rr >= d) {
-        q1 += 1;
-        rr -= d;
-    }
-    r = rr;
-    return q1;
-}
-
-// The shifted inverse starts at the largest scheduled precision up to this
-// many limbs, computed by recip_longdiv instead of Newton steps.
-constexpr int DIV_LONGDIV_MAX = 10;
-
-// Y[0..n] = floor((B^(2n) - 1) / D) for D = the top n limbs of the
-// normalised divisor (Vn[K-n .. K-1], zeros below when K < n): a shifted
-// inverse at precision n computed directly by schoolbook long division
-// (Knuth, TAOCP vol. 2, 4.3.1, Algorithm D) with 2-by-1 quotient estimates.
-// One thread; u holds 2n + 1 limbs of scratch.  vr = recip_limb(Vn[K-1]).
-// Kept out of line and as a plain loop: it runs once per division, where a
-// compact body costs fewer instruction fetches than an unrolled one.
-__device__ __noinline__ static void recip_longdiv(uint64_t* Y, int n, const uint64_t* Vn, int K, uint64_t vr,
-                                                  uint64_t* u) {
-    auto D = [&](int i) -> uint64_t {
-        const int src = K - n + i;
-        return src >= 0 ? Vn[src] : 0;
-    };
-    for (int i = 0; i < 2 * n; i++) u[i] = ~0ull;
-    u[2 * n] = 0;
-    const uint64_t d1 = D(n - 1), d2 = n >= 2 ? D(n - 2) : 0;
-    for (int j = n; j >= 0; j--) {
-        const uint64_t u2 = u[j + n], u1 = u[j + n - 1], u0 = (j + n >= 2) ? u[j + n - 2] : 0;
-        uint64_t qh, rh;
-        bool rh_over = false;
-        if (u2 >= d1) {                  // u2 == d1: q-hat = B - 1, r-hat = u1 + d1
-            qh = ~0ull;
-            rh = u1 + d1;
-            rh_over = rh < u1;
-        } else {
-            qh = div_2by1(u2, u1, d1, vr, rh);
-        }
-        for (int t = 0; t < 2 && !rh_over; t++) {   // q-hat * d2 > r-hat * B + u0: one too large
-            const uint64_t p_lo = qh * d2, p_hi = __umul64hi(qh, d2);
-            if (p_hi > rh || (p_hi == rh && p_lo > u0)) {
-                qh -= 1;
-                const uint64_t nr = rh + d1;
-                rh_over = nr < rh;
-                rh = nr;
-            } else {
-                break;
-            }
-        }
-        // u[j .. j+n] -= q-hat * D
-        uint64_t carry = 0, borrow = 0;
-        for (int i = 0; i < n; i++) {
-            const uint64_t d = D(i);
-            const uint64_t plo = qh * d, phi = __umul64hi(qh, d);
-            const uint64_t sub = plo + carry;
-            carry = phi + (sub < plo ? 1 : 0);
-            const uint64_t x = u[j + i];
-            const uint64_t y = x - sub;
-            const uint64_t b1 = x < sub ? 1 : 0;
-            u[j + i] = y - borrow;
-            borrow = b1 | (y < borrow ? 1 : 0);
-        }
-        const uint64_t x = u[j + n];
-        const uint64_t y = x - carry;
-        const uint64_t b1 = x < carry ? 1 : 0;
-        u[j + n] = y - borrow;
-        const bool neg = (b1 | (y < borrow ? 1 : 0)) != 0;
-        if (neg) {                       // one too large after all: add D back
-            qh -= 1;
-            uint64_t c = 0;
-            for (int i = 0; i < n; i++) {
-                const uint64_t d = D(i);
-                const uint64_t s = u[j + i] + d;
-                const uint64_t c1 = s < d ? 1 : 0;
-                const uint64_t s2 = s + c;
-                c = c1 | (s2 < s ? 1 : 0);
-                u[j + i] = s2;
-            }
-            u[j + n] += c;
-        }
-        Y[j] = qh;
-    }
-}
-
-// Newton steps up to this precision (limbs) run on warp 0 alone
-// (WarpGroup): their operands are small, and one warp with __syncwarp
-// finishes them sooner than the whole CTA with its barriers.
 constexpr int DIV_WARP_NEWTON_MAX = 64;
+// The first iterate of the shifted inverse comes from long division up to
+// this precision (limbs; div_warp<2> holds divisors up to 64 limbs).
+constexpr int DIV_INIT_LONG_MAX = 64;
 
 // One Newton step of the shifted inverse, from precision p to pn: Y_p (p + 1
 // limbs at Yb + (Pmax - p)) becomes Y_pn (pn + 1 limbs at Yb + (Pmax - pn)).
@@ -269,19 +118,30 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
             sched[ns++] = x;
         }
     }
-    // start at p0, the largest scheduled precision <= DIV_LONGDIV_MAX, by long division
-    int p0 = 1;
+    // start at p0, the largest scheduled precision <= DIV_INIT_LONG_MAX:
+    // Y_p0 = floor((B^(2 p0) - 1) / D) for D = the top p0 limbs of v, by long
+    // division on one warp (divsmall.cuh) -- about p0 quotient limbs of a few
+    // hundred cycles each, where the Newton steps it replaces cost a block
+    // product and barriers each
+    int p0 = 2;
     for (int si = 0; si < ns; si++)
-        if (sched[si] <= DIV_LONGDIV_MAX && sched[si] > p0) p0 = sched[si];
-    if (rk == 0) {
-        const uint64_t vr = recip_limb(Vn[K - 1]);
-        if (p0 == 1) {
-            Yb[Pmax - 1] = vr;
-            Yb[Pmax] = 1;
-        } else {
-            recip_longdiv(Yb + (Pmax - p0), p0, Vn, K, vr, X + g.oProd);
-        }
-        Yb[Pmax + 1] = 0;
+        if (sched[si] <= DIV_INIT_LONG_MAX && sched[si] > p0) p0 = sched[si];
+    const bool init_warp = std::is_same<Grp, CtaGroup>::value ? threadIdx.x < 32 : true;
+    if (init_warp) {
+        auto ld_u = [](uint32_t) { return ~0ull; };
+        auto ld_v = [&](uint32_t i) -> uint64_t {
+            const int src = K - p0 + (int)i;
+            return src >= 0 ? Vn[src] : 0;
+        };
+        auto st_q = [&](uint32_t i, uint64_t x) {
+            if (i <= (uint32_t)p0) Yb[Pmax - p0 + i] = x;   // the quotient has p0 + 1 limbs
+        };
+        auto st_r = [](uint32_t, uint64_t) {};
+        if (p0 <= 32)
+            div_warp<1>(2 * (uint32_t)p0, (uint32_t)p0, ld_u, ld_v, st_q, st_r);
+        else
+            div_warp<2>(2 * (uint32_t)p0, (uint32_t)p0, ld_u, ld_v, st_q, st_r);
+        if ((threadIdx.x & 31) == 0) Yb[Pmax + 1] = 0;
     }
     Grp::sync();
     int p = p0;

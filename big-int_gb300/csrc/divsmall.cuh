@@ -1,7 +1,7 @@
 // divsmall.cuh -- division of one instance by one thread, for divisors of at
 // most 16 64-bit limbs: schoolbook long division (Knuth, TAOCP vol. 2,
 // 4.3.1, Algorithm D) with 2-by-1 quotient estimates (Moller and Granlund's
-// reciprocal, divcore.cuh).  The quotient and remainder of u / v are unique,
+// reciprocal, divlimb.cuh).  The quotient and remainder of u / v are unique,
 // so the results are the ones the shifted-inverse division (divcore.cuh, the
 // reference's algorithm) gives; what changes is the cost.  Long division does
 // (MU - K + 1) K limb products for a K-limb divisor, about one multiply's
@@ -17,7 +17,7 @@
 #pragma once
 
 #include "chain.cuh"
-#include "divcore.cuh"
+#include "divlimb.cuh"
 
 namespace bi {
 

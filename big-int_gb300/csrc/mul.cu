@@ -26,12 +26,20 @@
 //   * The windows overlap by two limbs; a carry-lookahead across windows
 //     (block_carry_in) merges them, as the reference's final baddKer3Run
 //     merges its low/high/carry vectors (ker-mul.cu.h:588-645).
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "mulcore.cuh"
 
 namespace bi {
 
+constexpr uint32_t MUL_CTA_MAX_THREADS = 512;   // the CTA multiply's launch bound
+
 template <typename T, int C, bool FULL>
-__global__ void __launch_bounds__(512)
+__global__ void __launch_bounds__(MUL_CTA_MAX_THREADS)
 mul_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, uint64_t n, MulGeom g,
            FastDiv lpdiv) {
     extern __shared__ __align__(16) uint64_t smem[];
@@ -309,19 +317,71 @@ static bi_status mul_warp(const T* a, const T* b, T* r, uint32_t m, uint64_t n, 
 constexpr uint32_t MUL_MAX_L = 4096;   // u64-view limbs per operand
 constexpr uint32_t MUL_WARP_MAX_L = 32;    // full products up to here take the warp kernel
 
+// ---------------------------------------------------------------------------
+// Tiling of the CTA multiply: instances per CTA (ipc) and row slices per
+// window pair (S).  Without a tuning entry the library's own choice applies
+// (as many instances as fill MUL_CTA_THREADS threads, fewer when the batch is
+// small, no slicing); bi_mul_autotune_* times the candidates on the caller's data and
+// records the fastest here, per device, limb width, product kind and size.
+// ---------------------------------------------------------------------------
+struct MulTune {
+    uint32_t ipc, S;
+};
+
+// The default CTA size: the autotuner's sweep on GB300 (full products, m =
+// 64..2048 64-bit limbs) found 128-thread CTAs best or within 1 % of best at
+// every size, 256-thread CTAs 2-7 % slower.
+constexpr uint32_t MUL_CTA_THREADS = 128;
+
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, uint32_t>, MulTune> g_tune;   // (device, limb bytes, full, L)
+
+static bool mul_tuning_lookup(int limb_bytes, bool full, uint32_t L, MulTune* t) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(std::make_tuple(dev, limb_bytes, full ? 1 : 0, L));
+    if (it == g_tune.end()) return false;
+    *t = it->second;
+    return true;
+}
+
+// The geometry of a tiling; false if it does not fit a CTA.
+static bool mul_geom_tiled(uint32_t L, bool full, uint32_t ipc, uint32_t S, MulGeom* out) {
+    if (ipc < 1 || S < 1 || S > 32 || (S & (S - 1))) return false;
+    MulGeom g = mul_geometry(L, full, ipc);
+    if (g.ipc != ipc) return false;              // more instances than 256 threads hold
+    g.S = S;
+    g.lgS = 0;
+    while ((1u << g.lgS) < S) g.lgS++;
+    if ((uint64_t)g.ipc * g.tpi * g.S > MUL_CTA_MAX_THREADS) return false;
+    if (mul_smem_bytes(g) > 227 * 1024) return false;
+    *out = g;
+    return true;
+}
+
 template <typename T, bool FULL>
-static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
-    constexpr int C = MUL_C;
-    const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
-    if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
-    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, st);
-    // at least two CTAs per SM when the batch is small: fewer instances per CTA
+static MulGeom mul_geom_for(uint32_t L, uint64_t n) {
+    MulTune t;
+    MulGeom g;
+    if (mul_tuning_lookup((int)sizeof(T), FULL, L, &t) && mul_geom_tiled(L, FULL, t.ipc, t.S, &g)) return g;
+    // CTAs of about MUL_CTA_THREADS threads (as many instances as fill them),
+    // fewer instances when the batch is small: at least two CTAs per SM
+    const uint32_t tpi = mul_geometry(L, FULL, 1).tpi;
+    uint32_t cap = MUL_CTA_THREADS / tpi;
+    if (cap < 1) cap = 1;
     const uint64_t fill = (n + 2ull * num_sms() - 1) / (2ull * num_sms());
-    MulGeom g = mul_geometry(L, FULL, fill < 256 ? (uint32_t)(fill ? fill : 1) : 256u);
+    if (fill < cap) cap = fill ? (uint32_t)fill : 1u;
+    return mul_geometry(L, FULL, cap);
+}
+
+template <typename T, bool FULL>
+static bi_status mul_launch_geom(const T* a, const T* b, T* r, uint32_t m, uint64_t n, MulGeom g, cudaStream_t st) {
+    constexpr int C = MUL_C;
     g.m = m;
     g.out_words = FULL ? 2 * m : m;
-    const uint32_t threads = (g.ipc * g.tpi + 31) / 32 * 32;
-    const size_t smem = (size_t)g.ipc * g.IS * 8 + 3 * 32 * 4;
+    const uint32_t threads = mul_threads(g);
+    const size_t smem = mul_smem_bytes(g);
     if (smem > 227 * 1024) return set_error(BI_EUNSUPPORTED, "mul: m=%u needs too much shared memory", m);
     auto kern = mul_kernel<T, C, FULL>;
     cudaError_t e = smem_opt_in((const void*)kern, smem);
@@ -330,6 +390,14 @@ static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n
     if (blocks > 0x7fffffffull) return set_error(BI_EINVAL, "mul: n too large");
     kern<<<(unsigned)blocks, threads, smem, st>>>(a, b, r, n, g, FastDiv(g.Lp));
     return check_launch(FULL ? "mulfull kernel" : "mul kernel");
+}
+
+template <typename T, bool FULL>
+static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
+    const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
+    if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
+    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, st);
+    return mul_launch_geom<T, FULL>(a, b, r, m, n, mul_geom_for<T, FULL>(L, n), st);
 }
 
 template <typename T, bool FULL>
@@ -368,6 +436,104 @@ static bi_status mul_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n,
     return check_launch("mul chain kernel");
 }
 
+// Time every tiling that fits (ipc in 1, 2, 4, ..., S in 1, 2, 4) on the
+// caller's operands, median of `reps` runs each, and record the fastest.
+template <typename T, bool FULL>
+static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t n, int reps, int* chosen,
+                              cudaStream_t st) {
+    if (chosen) chosen[0] = chosen[1] = 0;
+    const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
+    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, st);   // the warp kernel: nothing to tile
+    std::vector<std::pair<uint32_t, uint32_t>> cands;
+    for (uint32_t ipc = 1; ipc <= 64; ipc *= 2)
+        for (uint32_t S = 1; S <= 4; S *= 2) {
+            MulGeom g;
+            if (mul_geom_tiled(L, FULL, ipc, S, &g) && (uint64_t)ipc <= n) cands.push_back({ipc, S});
+        }
+    if (cands.empty()) return set_error(BI_EUNSUPPORTED, "mul autotune: no tiling fits m=%u", m);
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+        return set_error(BI_ECUDA, "mul autotune: %s", cudaGetErrorString(cudaGetLastError()));
+    float best = 1e30f;
+    MulTune pick = {0, 0};
+    bi_status st_out = BI_OK;
+    for (const auto& c : cands) {
+        MulGeom g;
+        mul_geom_tiled(L, FULL, c.first, c.second, &g);
+        std::vector<float> ts;
+        for (int k = 0; k <= reps && st_out == BI_OK; k++) {   // the first run warms up
+            cudaEventRecord(e0, st);
+            st_out = mul_launch_geom<T, FULL>(a, b, r, m, n, g, st);
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) st_out = set_error(BI_ECUDA, "mul autotune: %s",
+                                                                            cudaGetErrorString(cudaGetLastError()));
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (k > 0) ts.push_back(ms);
+        }
+        if (st_out != BI_OK) break;
+        std::sort(ts.begin(), ts.end());
+        const float med = ts[ts.size() / 2];
+        if (med < best) {
+            best = med;
+            pick = {c.first, c.second};
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st_out != BI_OK) return st_out;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[std::make_tuple(dev, (int)sizeof(T), FULL ? 1 : 0, L)] = pick;
+    }
+    // leave r as one plain call with the chosen tiling writes it
+    MulGeom g;
+    mul_geom_tiled(L, FULL, pick.ipc, pick.S, &g);
+    BI_RETURN_IF((mul_launch_geom<T, FULL>(a, b, r, m, n, g, st)));
+    if (chosen) {
+        chosen[0] = (int)pick.ipc;
+        chosen[1] = (int)pick.S;
+    }
+    return BI_OK;
+}
+
+template <typename T>
+static bi_status mul_autotune_entry(const T* a, const T* b, T* r, uint32_t m, uint64_t n, int full, int reps,
+                                    int* chosen, bi_stream s) {
+    if (n == 0) return set_error(BI_EINVAL, "mul autotune: n must be >= 1");
+    if (m == 0) return set_error(BI_EINVAL, "m must be >= 1");
+    if (reps < 1 || reps > 100) return set_error(BI_EINVAL, "mul autotune: reps must be in 1..100");
+    if (!a || !b || !r) return set_error(BI_EINVAL, "NULL buffer");
+    if ((uintptr_t)a % sizeof(T) || (uintptr_t)b % sizeof(T) || (uintptr_t)r % sizeof(T))
+        return set_error(BI_EINVAL, "buffers must be aligned to the limb size");
+    const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
+    if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
+    return full ? mul_autotune<T, true>(a, b, r, m, n, reps, chosen, (cudaStream_t)s)
+                : mul_autotune<T, false>(a, b, r, m, n, reps, chosen, (cudaStream_t)s);
+}
+
+static bi_status mul_set_tuning(int limb_bytes, uint32_t m, int full, int ipc, int slices) {
+    if (m == 0) return set_error(BI_EINVAL, "m must be >= 1");
+    const uint32_t L = limb_bytes == 8 ? m : (m + 1) / 2;
+    if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(dev, limb_bytes, full ? 1 : 0, L);
+    if (ipc == 0) {                                   // back to the library's own choice
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune.erase(key);
+        return BI_OK;
+    }
+    MulGeom g;
+    if (ipc < 0 || slices < 1 || !mul_geom_tiled(L, full != 0, (uint32_t)ipc, (uint32_t)slices, &g))
+        return set_error(BI_EINVAL, "mul tuning: ipc=%d slices=%d does not fit a CTA for m=%u", ipc, slices, m);
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = {(uint32_t)ipc, (uint32_t)slices};
+    return BI_OK;
+}
+
 }  // namespace bi
 
 using namespace bi;
@@ -385,6 +551,21 @@ bi_status bi_mul_chain_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, ui
 
 uint32_t bi_max_limbs_mul_u64(void) { return MUL_MAX_L; }
 uint32_t bi_max_limbs_mul_u32(void) { return 2 * MUL_MAX_L; }
+
+bi_status bi_mul_autotune_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n, int full,
+                              int reps, int* chosen, bi_stream s) {
+    return mul_autotune_entry<uint64_t>(a, b, r, m, n, full, reps, chosen, s);
+}
+bi_status bi_mul_autotune_u32(const uint32_t* a, const uint32_t* b, uint32_t* r, uint32_t m, uint64_t n, int full,
+                              int reps, int* chosen, bi_stream s) {
+    return mul_autotune_entry<uint32_t>(a, b, r, m, n, full, reps, chosen, s);
+}
+bi_status bi_mul_set_tuning_u64(uint32_t m, int full, int ipc, int slices) {
+    return mul_set_tuning(8, m, full, ipc, slices);
+}
+bi_status bi_mul_set_tuning_u32(uint32_t m, int full, int ipc, int slices) {
+    return mul_set_tuning(4, m, full, ipc, slices);
+}
 
 bi_status bi_mul_u64(const uint64_t* a, const uint64_t* b, uint64_t* r, uint32_t m, uint64_t n, bi_stream s) {
     return mul_entry<uint64_t, false>(a, b, r, m, n, s);

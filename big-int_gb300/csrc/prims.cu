@@ -17,7 +17,8 @@
 //     the 2-by-1 division by a precomputed reciprocal of Moller and Granlund
 //     ("Improved division by invariant integers", IEEE Trans. Computers
 //     60(2), 2011, Algorithm 4), on the u64 view of the instance.
-#include "divcore.cuh"   // recip_limb, div_2by1
+#include "common.cuh"
+#include "divlimb.cuh"   // recip_limb, div_2by1
 
 namespace bi {
 

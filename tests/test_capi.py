@@ -69,6 +69,18 @@ def test_invalid_arguments_rejected_before_launch(L):
     assert L.bi_add_u64(fake, fake, fake, big, 1, None) == 6         # unsupported size
 
 
+def test_mul_tuning_arguments_checked_on_host(L):
+    assert L.bi_mul_set_tuning_u64(0, 1, 4, 1) == 1                  # m == 0
+    assert L.bi_mul_set_tuning_u64(64, 1, 4, 3) == 1                 # slices not a power of two
+    assert L.bi_mul_set_tuning_u64(64, 1, 4096, 1) == 1              # more instances than a CTA holds
+    assert L.bi_mul_set_tuning_u64(64, 1, -1, 1) == 1
+    assert L.bi_mul_set_tuning_u64(1 << 20, 1, 1, 1) == 6            # unsupported size
+    fake = ctypes.c_void_p(0x1000)
+    assert L.bi_mul_autotune_u64(fake, fake, fake, 64, 0, 1, 3, None, None) == 1   # n == 0
+    assert L.bi_mul_autotune_u64(fake, fake, fake, 64, 8, 1, 0, None, None) == 1   # reps == 0
+    assert L.bi_mul_autotune_u64(None, fake, fake, 64, 8, 1, 3, None, None) == 1   # NULL
+
+
 def test_library_built_for_sm103a():
     import bigint_gb300 as B
 
