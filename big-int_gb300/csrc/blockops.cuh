@@ -1,8 +1,8 @@
 // blockops.cuh -- CTA-cooperative big-integer primitives on shared memory.
 //
-// Every function here is called by all threads of a cooperating group -- the
-// whole CTA (CtaGroup, the default) or one warp (WarpGroup) -- with the same
-// arguments, and synchronises that group.  Limbs are 64-bit, little-endian.  These are the batched-division building blocks:
+// Every function here is called by all threads of a cooperating group (the
+// whole CTA: CtaGroup, the default) with the same arguments, and synchronises
+// that group.  Limbs are 64-bit, little-endian.  These are the batched-division building blocks:
 // the reference's division prototype composes the same primitives (shift,
 // compare, findk, add, sub, mult; prototypes/div.c:49-218, and their parallel
 // forms in futhark/helper.fut:101-124 and futhark/div.fut:21-69).
@@ -59,9 +59,8 @@ __device__ __forceinline__ uint32_t block_max_u32(uint32_t v, uint32_t* scratch)
 }
 
 // The threads that cooperate on one number.  CtaGroup: the whole CTA, with
-// __syncthreads and shared-memory exchanges through `scratch`.  WarpGroup: the
-// calling warp alone (other warps may be doing anything), with __syncwarp,
-// ballots and shuffles -- no CTA barrier.
+// __syncthreads and shared-memory exchanges through `scratch`.  (Work on one
+// warp -- small products, long division -- has its own kernels.)
 struct CtaGroup {
     static __device__ __forceinline__ int rank() { return (int)threadIdx.x; }
     static __device__ __forceinline__ int size() { return (int)blockDim.x; }
@@ -79,26 +78,6 @@ struct CtaGroup {
         const uint32_t r = scratch[100];
         __syncthreads();
         return r;
-    }
-};
-
-struct WarpGroup {
-    static __device__ __forceinline__ int rank() { return (int)(threadIdx.x & 31); }
-    static __device__ __forceinline__ int size() { return 32; }
-    static __device__ __forceinline__ void sync() { __syncwarp(); }
-    static __device__ __forceinline__ uint32_t carry_in(uint32_t g, uint32_t p, bool seg, uint32_t*) {
-        const uint32_t kill = __ballot_sync(0xffffffffu, seg) >> 1;
-        const uint32_t A = __ballot_sync(0xffffffffu, g | p) & ~kill;
-        const uint32_t B = __ballot_sync(0xffffffffu, g) & ~kill;
-        return (warp_carry_resolve(A, B, 0).carries >> (threadIdx.x & 31)) & 1u;
-    }
-    static __device__ __forceinline__ uint32_t max_u32(uint32_t v, uint32_t*) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-        return v;
-    }
-    static __device__ __forceinline__ uint32_t bcast(uint32_t v, int src, uint32_t*) {
-        return __shfl_sync(0xffffffffu, v, src);
     }
 };
 

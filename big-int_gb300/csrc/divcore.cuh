@@ -23,7 +23,6 @@ struct DivGeom {
     uint32_t smem_limbs;
 };
 
-constexpr int DIV_WARP_NEWTON_MAX = 64;
 // The first iterate of the shifted inverse comes from long division up to
 // this precision (limbs; div_warp<2> holds divisors up to 64 limbs).
 constexpr int DIV_INIT_LONG_MAX = 64;
@@ -145,26 +144,6 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
     }
     Grp::sync();
     int p = p0;
-    if constexpr (std::is_same<Grp, CtaGroup>::value) {
-        // the small steps on warp 0 alone, then one barrier
-        if (threadIdx.x < 32) {
-            int pw = p0;
-            for (int si = ns - 1; si >= 0; si--) {
-                const int pn = sched[si];
-                if (pn <= pw) continue;
-                if (pn > DIV_WARP_NEWTON_MAX) break;
-                newton_step<WarpGroup>(g, Vn, K, Yb, X, scratch, pw, pn);
-                pw = pn;
-            }
-        }
-        __syncthreads();
-        for (int si = ns - 1; si >= 0; si--) {     // where warp 0 stopped
-            const int pn = sched[si];
-            if (pn <= p) continue;
-            if (pn > DIV_WARP_NEWTON_MAX) break;
-            p = pn;
-        }
-    }
     for (int si = ns - 1; si >= 0; si--) {
         const int pn = sched[si];
         if (pn <= p) continue;
