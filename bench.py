@@ -854,7 +854,29 @@ def run_ours(args) -> None:
             dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
         e2e = {"value": round(per_step * e2e_steps * world / (float(e2e_t.item()) / 1e3) / 1e9, 2), "unit": "GB/s",
                "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
-               "path": "bi_host_add_u64 / bi_host_sub_u64 (chunked, 3-stream pipeline) from pinned host buffers"}
+               "path": "bi_host_add_u64 / bi_host_sub_u64 from pinned host buffers (the kernels read and write "
+                       "them in place over the CPU-GPU link)"}
+        # the link's own ceiling for this traffic: copy-engine bandwidth each way on the same pinned buffers
+        dev = torch.empty(total, dtype=torch.int64, device="cuda")
+        def copy_gbs(dst, src):
+            for _ in range(2):
+                dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                dst.copy_(src, non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize()
+            return 3 * total * 8 / (e0.elapsed_time(e1) / 1e3) / 1e9
+        h2d_gbs, d2h_gbs = copy_gbs(dev, ha), copy_gbs(hr, dev)
+        del dev
+        t_min = max(h2d / e2e_steps / (h2d_gbs * 1e9), d2h / e2e_steps / (d2h_gbs * 1e9))
+        e2e["link"] = {"h2d_gbs": round(h2d_gbs, 1), "d2h_gbs": round(d2h_gbs, 1),
+                       "ceiling_gbs": round(per_step / t_min / 1e9, 1),
+                       "frac": round(e2e["value"] / (per_step / t_min / 1e9), 3),
+                       "note": "ceiling = the step's algorithmic bytes / the longer of its host-to-device and "
+                               "device-to-host bytes at the measured copy bandwidths (both directions overlapped)"}
 
     extra = None
     if not args.no_extras:

@@ -292,9 +292,10 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
 #pragma unroll
             for (int i = 1; i < VPL; i++) Hs[i] = __umul64hi(qh, D[i - 1]);
             const uint32_t gA = chain_sub<VPL>(R, Hs, 0);
-            bool zA = true;
+            uint64_t orA = 0;   // the lane's block is zero: one compare of the OR of its limbs
 #pragma unroll
-            for (int i = 0; i < VPL; i++) zA &= R[i] == 0;
+            for (int i = 0; i < VPL; i++) orA |= R[i];
+            const bool zA = orA == 0;
             const uint32_t binA = (uint32_t)warp_chain_in(gA != 0, zA, coutA);
             const uint64_t th = __shfl_sync(FULL, htop, 31);
             const uint64_t x = rtop - th;
@@ -307,9 +308,10 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
 #pragma unroll
             for (int i = 0; i < VPL; i++) Ls[i] = qh * D[i];
             const uint32_t gB = chain_sub<VPL>(R, Ls, binA) & (zA && binA ? 0u : 1u);
-            bool zB = true;
+            uint64_t orB = 0;
 #pragma unroll
-            for (int i = 0; i < VPL; i++) zB &= R[i] == 0;
+            for (int i = 0; i < VPL; i++) orB |= R[i];
+            const bool zB = orB == 0;
             uint32_t bin = (uint32_t)warp_chain_in(gB != 0, zB, coutB);
             uint64_t Z[VPL];
 #pragma unroll
