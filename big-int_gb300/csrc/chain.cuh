@@ -93,6 +93,23 @@ __device__ __forceinline__ uint32_t chain_sub(uint64_t (&x)[N], const uint64_t (
     }
 }
 
+// x = x - (gen(0), gen(1), ...) - c over N limbs, the subtrahend produced
+// eight limbs at a time just before its chain block, so that no more than
+// eight of its limbs are live at once.
+template <int N, typename Gen>
+__device__ __forceinline__ uint32_t chain_sub_from(uint64_t (&x)[N], Gen gen, uint32_t c) {
+    constexpr int Bk = N < 8 ? N : 8;
+    static_assert(N % Bk == 0, "chain_sub_from: N must be 1, 2, 4 or a multiple of 8");
+#pragma unroll
+    for (int b = 0; b < N / Bk; b++) {
+        uint64_t y[Bk];
+#pragma unroll
+        for (int j = 0; j < Bk; j++) y[j] = gen(b * Bk + j);
+        c = chain_sub<Bk>(*reinterpret_cast<uint64_t(*)[Bk]>(&x[b * Bk]), y, c);
+    }
+    return c;
+}
+
 // The carry out alone (x and y unchanged): the same chain on copies.
 template <typename T>
 __device__ __forceinline__ uint32_t chain_add8_cout(const T (&x)[8], const T (&y)[8], uint32_t c) {

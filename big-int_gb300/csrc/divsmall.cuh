@@ -25,7 +25,6 @@ constexpr int DIV_THREAD_MAX_MV = 16;   // 64-bit divisor limbs handled by div_t
 constexpr int DIV_THREAD_CTA = 64;      // threads per CTA of the one-thread-per-instance kernels
 constexpr int DIV_WARP_MAX_MV = 1024;   // 64-bit divisor limbs handled by div_warp
 constexpr int DIV_WARP_CTA = 128;       // threads per CTA of the one-warp-per-instance kernels
-
 // Long division on warps or the shifted inverse on CTAs, for a batch of n
 // instances with MV-limb divisors (64-bit limbs) on a GPU of `sms` SMs.
 // Long division does fewer limb products but runs one quotient limb after
@@ -234,6 +233,7 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
     }
     const uint64_t d1 = __shfl_sync(FULL, D[VPL - 1], 31);
     const uint64_t d2 = VPL >= 2 ? __shfl_sync(FULL, D[VPL >= 2 ? VPL - 2 : 0], 31) : __shfl_sync(FULL, D[0], 30);
+    auto Dv = [&](int i) -> uint64_t { return D[i]; };
     const uint64_t vr = recip_limb(d1);
 
     // the shifted dividend: sh(t) = limb t of u 2^s, t in [0, MU]
@@ -285,13 +285,11 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
         uint64_t coutA, coutB;
         bool neg;
         {
-            const uint64_t htop = __umul64hi(qh, D[VPL - 1]);
+            const uint64_t htop = __umul64hi(qh, Dv(VPL - 1));
             const uint64_t hb = __shfl_up_sync(FULL, htop, 1);
-            uint64_t Hs[VPL];
-            Hs[0] = lane == 0 ? 0 : hb;
-#pragma unroll
-            for (int i = 1; i < VPL; i++) Hs[i] = __umul64hi(qh, D[i - 1]);
-            const uint32_t gA = chain_sub<VPL>(R, Hs, 0);
+            const uint64_t h0 = lane == 0 ? 0 : hb;
+            const uint32_t gA = chain_sub_from<VPL>(
+                R, [&](int i) { return i == 0 ? h0 : __umul64hi(qh, Dv(i > 0 ? i - 1 : 0)); }, 0);
             uint64_t orA = 0;   // the lane's block is zero: one compare of the OR of its limbs
 #pragma unroll
             for (int i = 0; i < VPL; i++) orA |= R[i];
@@ -304,19 +302,14 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
             // pass B: R -= low halves of q-hat D and the borrow from pass A;
             // a lane of zeros that took A's borrow wrapped to all ones, which
             // A's ballots already carried on, so it generates no B borrow
-            uint64_t Ls[VPL];
-#pragma unroll
-            for (int i = 0; i < VPL; i++) Ls[i] = qh * D[i];
-            const uint32_t gB = chain_sub<VPL>(R, Ls, binA) & (zA && binA ? 0u : 1u);
+            const uint32_t gB = chain_sub_from<VPL>(R, [&](int i) { return qh * Dv(i); }, binA) &
+                                (zA && binA ? 0u : 1u);
             uint64_t orB = 0;
 #pragma unroll
             for (int i = 0; i < VPL; i++) orB |= R[i];
             const bool zB = orB == 0;
             uint32_t bin = (uint32_t)warp_chain_in(gB != 0, zB, coutB);
-            uint64_t Z[VPL];
-#pragma unroll
-            for (int i = 0; i < VPL; i++) Z[i] = 0;
-            chain_sub<VPL>(R, Z, bin);
+            chain_sub_from<VPL>(R, [](int) { return 0ull; }, bin);
             const bool bB = rtop < coutB;
             rtop -= coutB;
             neg = bA || bB;                    // at most one of the two wraps
@@ -327,8 +320,9 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
             bool allo = true;
 #pragma unroll
             for (int i = 0; i < VPL; i++) {
-                const uint64_t x = R[i] + D[i];
-                const uint64_t c1 = x < D[i] ? 1 : 0;
+                const uint64_t di = Dv(i);
+                const uint64_t x = R[i] + di;
+                const uint64_t c1 = x < di ? 1 : 0;
                 const uint64_t y = x + cy;
                 cy = c1 | (y < x ? 1 : 0);
                 R[i] = y;
