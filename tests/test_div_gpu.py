@@ -131,6 +131,28 @@ def test_method_boundaries(bigint, oracle, mu, mv):
             _run(bigint, oracle, u, v, method)
 
 
+@pytest.mark.parametrize("method", ["auto", "long", "shinv"])
+@pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
+@pytest.mark.parametrize("mu,mv", [(2048, 1), (1000, 3), (700, 16), (700, 17), (1999, 40), (1500, 100), (2048, 513)])
+def test_long_dividend_short_divisor(bigint, oracle, dtype, mu, mv, method):
+    """Dividends many times longer than the divisor: the long divisions stream
+    hundreds of dividend limbs through their window (the warp kernel reloads
+    its 32-limb buffer dozens of times), with ragged u32 sizes."""
+    if dtype == np.uint32:
+        mu, mv = 2 * mu - 1, 2 * mv - 1     # odd word counts: a half-filled top 64-bit limb
+    n = 6
+    u = uniform_limbs(1300 + mu, n, mu, dtype)
+    v = uniform_limbs(1400 + mv, n, mv, dtype)
+    v[:, -1] |= 1
+    top = np.iinfo(dtype).max
+    u[0] = top
+    v[0] = top                         # all-ones operands
+    u[1, mu // 2:] = 0                 # a dividend half as long
+    v[2, :] = 0
+    v[2, 0] = 1                        # v = 1: q = u
+    _run(bigint, oracle, u, v, method)
+
+
 def _addback_rows(seed, mu, mv, n, bits):
     """u = (qh v - 1) B^(mu - mv - 1) + low with v normalised: the quotient
     estimate from the top limbs is qh, one more than the true top limb, so the
