@@ -16,10 +16,10 @@
 //     long division (divsmall.cuh) on one thread per instance for divisors
 //     up to 4, 8 and 16 limbs, on one warp per instance up to 32, 64, ...,
 //     1024 limbs (the register arrays sized for the class), and the shifted
-//     inverse (divcore.cuh) on one 512-thread CTA per instance above; most
-//     expensive first within a class.  A batch holds many divisions of each
-//     class, where long division's throughput wins (uniform batches choose
-//     per call, div.cu).
+//     inverse (divcore.cuh) on one 512-thread CTA per instance above -- and
+//     for a class above 128 limbs with too few divisions to fill the GPU,
+//     the crossover a uniform batch uses (div_use_long); most expensive
+//     first within a class.
 // The persistent kernels run concurrently on forked streams; the fork,
 // the launches, the counter reset and the join are captured once into a CUDA
 // graph and replayed by every bi_plan_execute.  Work is handed out with one
@@ -279,15 +279,31 @@ static size_t mul_smem_for(const bi_plan* p, int ipc_div) {
     return best;
 }
 
-// Division order: by size class, then most expensive first.
-static bool div_before(const bi_desc& x, const bi_desc& y) {
-    const int cx = div_class(x.mb), cy = div_class(y.mb);
+// The class of each division: by divisor size (div_class), except that a
+// warp class with too few divisions for long division's throughput to win
+// (div_use_long, the same measured crossover as a uniform batch) goes to the
+// shifted inverse on CTAs.  map[c] is the class that size class c runs as.
+static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n, int sms, int* map) {
+    uint64_t cnt[DIV_CLASSES] = {};
+    for (uint32_t k = 0; k < n; k++) cnt[div_class(descs[div[k]].mb)]++;
+    for (int c = 0; c < DIV_CLASSES; c++) {
+        map[c] = c;
+        if (c >= DIV_THREAD_CLASSES && c < DIV_CTA_CLASS) {
+            const uint32_t max_mv = 32u << (c - DIV_THREAD_CLASSES);   // the class's largest divisor
+            if (!div_use_long(max_mv, cnt[c], sms)) map[c] = DIV_CTA_CLASS;
+        }
+    }
+}
+
+// Division order: by class, then most expensive first.
+static bool div_before(const bi_desc& x, const bi_desc& y, const int* map) {
+    const int cx = map[div_class(x.mb)], cy = map[div_class(y.mb)];
     if (cx != cy) return cx < cy;
     return (uint64_t)x.m * x.mb > (uint64_t)y.m * y.mb;
 }
 
 // Per-class offsets, counts and shared memory of a division list sorted by div_before.
-static void div_classes(bi_plan* p, const bi_desc* descs, const uint32_t* div, uint32_t n) {
+static void div_classes(bi_plan* p, const bi_desc* descs, const uint32_t* div, uint32_t n, const int* map) {
     p->div_smem = 0;
     for (int c = 0; c < DIV_CLASSES; c++) {
         p->div_off[c] = 0;
@@ -296,7 +312,7 @@ static void div_classes(bi_plan* p, const bi_desc* descs, const uint32_t* div, u
     }
     for (uint32_t k = 0; k < n; k++) {
         const bi_desc& d = descs[div[k]];
-        const int c = div_class(d.mb);
+        const int c = map[div_class(d.mb)];
         if (p->n_divc[c]++ == 0) p->div_off[c] = k;
         if (c == DIV_CTA_CLASS) p->divc_smem[c] = std::max(p->divc_smem[c], div_smem_bytes(div_geom(d.m, d.mb, 8)));
         p->div_smem = std::max(p->div_smem, p->divc_smem[c]);
@@ -523,7 +539,9 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     }
     // largest first: long instances start early, short ones fill the tail
     std::stable_sort(addsub.begin(), addsub.end(), [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
-    std::stable_sort(div.begin(), div.end(), [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y]); });
+    int dmap[DIV_CLASSES];
+    div_class_map(descs, div.data(), (uint32_t)div.size(), num_sms(), dmap);
+    std::stable_sort(div.begin(), div.end(), [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y], dmap); });
     std::stable_sort(mulkeys.begin(), mulkeys.end(), [](const std::pair<uint64_t, uint32_t>& x,
                                                         const std::pair<uint64_t, uint32_t>& y) {
         return x.first > y.first;
@@ -551,7 +569,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     p->n_mul = (uint32_t)mul.size();
     p->n_items = (uint32_t)items.size();
     p->n_div = (uint32_t)div.size();
-    div_classes(p, descs, div.data(), p->n_div);
+    div_classes(p, descs, div.data(), p->n_div, dmap);
     if (p->div_smem > 227 * 1024 || mul_smem_for(p, 1) > 227 * 1024) {
         plan_free(p);
         return set_error(BI_EUNSUPPORTED, "batch sizes need too much shared memory");
@@ -798,7 +816,9 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
         }
     }
     std::stable_sort(na_add, na_add + na, [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
-    std::stable_sort(na_div, na_div + nd, [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y]); });
+    int dmap[DIV_CLASSES];
+    div_class_map(descs, na_div, nd, num_sms(), dmap);
+    std::stable_sort(na_div, na_div + nd, [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y], dmap); });
     std::stable_sort(na_keys, na_keys + nk, [](const std::pair<uint64_t, uint32_t>& x,
                                                const std::pair<uint64_t, uint32_t>& y) { return x.first > y.first; });
     for (uint32_t k = 0; k < nk;) {
@@ -823,7 +843,7 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
     p.n_mul = nm;
     p.n_items = ni;
     p.n_div = nd;
-    div_classes(&p, descs, na_div, nd);
+    div_classes(&p, descs, na_div, nd, dmap);
     if (p.div_smem > 227 * 1024 || mul_smem_for(&p, 1) > 227 * 1024)
         return set_error(BI_EUNSUPPORTED, "batch sizes need too much shared memory");
     p.d_descs = (bi_desc*)(base + NA_DESC_OFF);

@@ -123,6 +123,36 @@ def test_large_instances(bigint, oracle):
     plan.close()
 
 
+def test_division_classes_by_count(bigint, oracle):
+    """Large-divisor classes run long division on warps when they hold many
+    divisions and the shifted inverse on CTAs when they hold few: 400
+    divisions of 400/200 limbs (above two per SM: warps) beside 6 of
+    1200/600 limbs (CTAs) and 40 of 60/20 limbs (warps, always)."""
+    B = bigint
+    rows = []
+    arena = []
+    off = 0
+    out = 0
+    seed = 900
+    for m, mb, count in [(400, 200, 400), (1200, 600, 6), (60, 20, 40)]:
+        for _ in range(count):
+            a = B.workloads.uniform_limbs(seed, 1, m)[0]
+            b = B.workloads.uniform_limbs(seed + 1, 1, mb)[0]
+            seed += 2
+            b[-1] |= np.uint64(1)
+            rows.append((m, mb, off, off + m, out))
+            arena += [a, b]
+            off += m + mb
+            out += m + mb
+    d = np.zeros(len(rows), dtype=B.DESC_DTYPE)
+    for i, (m, mb, ao, bo, ro) in enumerate(rows):
+        d[i] = (B.OP_DIV, m, mb, 0, ao, bo, ro, ro + m, i)
+    ar = np.concatenate(arena)
+    plan, din, dout, dfl = _run(B, d, ar, out, len(d))
+    check_batch(B, oracle, d, ar, B.to_host(dout, np.uint64), dfl.cpu().numpy())
+    plan.close()
+
+
 def test_batch_matches_per_size_kernels(bigint):
     """The batch and the plain one-launch-per-size kernels give the same results."""
     import torch
