@@ -14,8 +14,10 @@
 //     bucket item (as many instances as fit one CTA, mulcore.cuh);
 //   * divisions go to persistent kernels by divisor size class: schoolbook
 //     long division (divsmall.cuh) on one thread per instance for divisors
-//     up to 4, 8 and 16 limbs, on one warp per instance up to 32, 64, ...,
-//     1024 limbs (the register arrays sized for the class), and the shifted
+//     up to 4, 8 and 16 limbs, on one lane group per instance up to 32, 64,
+//     ..., 1024 limbs (8 lanes up to 64 limbs, 16 up to 128, a warp above:
+//     the register arrays sized for the class, the group size measured
+//     fastest in the batch), and the shifted
 //     inverse (divcore.cuh) on one 512-thread CTA per instance above -- and
 //     for a class above 128 limbs with too few divisions to fill the GPU,
 //     the crossover a uniform batch uses (div_use_long); most expensive
@@ -190,6 +192,35 @@ batch_divwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restri
     }
 }
 
+// Several divisions a warp, one per G-lane group (div_group): lane 0 takes
+// 32 / G list entries at a time.
+template <int VPL, int G>
+__global__ void __launch_bounds__(DIV_WARP_CTA)
+batch_divgroup_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                      uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    constexpr uint32_t ipw = 32 / G;
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(counter, ipw);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= count) break;
+        const uint32_t idx = base + lane / G;
+        const bool valid = idx < count;
+        bi_desc d = {};
+        if (valid) d = descs[list[idx]];
+        const uint64_t* u = in + d.a;
+        const uint64_t* v = in + d.b;
+        uint64_t* q = out + d.r;
+        uint64_t* r = out + d.r2;
+        const uint8_t st = div_group<VPL, G>(
+            valid, valid ? d.m : 1u, valid ? d.mb : 1u, [&](uint32_t i) { return u[i]; },
+            [&](uint32_t i) { return v[i]; }, [&](uint32_t i, uint64_t x) { q[i] = x; },
+            [&](uint32_t i, uint64_t x) { r[i] = x; });
+        if (flags && valid && (lane & (G - 1)) == 0) flags[d.flag] = st;
+    }
+}
+
 // At most 128 registers a thread, so 512 / THREADS CTAs fit an SM's register file.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS)
@@ -342,9 +373,9 @@ static const void* div_class_kernel(int c, int* threads) {
     case 0: return (const void*)batch_divthread_kernel<4>;
     case 1: return (const void*)batch_divthread_kernel<8>;
     case 2: return (const void*)batch_divthread_kernel<16>;
-    case 3: return (const void*)batch_divwarp_kernel<1>;
-    case 4: return (const void*)batch_divwarp_kernel<2>;
-    case 5: return (const void*)batch_divwarp_kernel<4>;
+    case 3: return (const void*)batch_divgroup_kernel<4, 8>;
+    case 4: return (const void*)batch_divgroup_kernel<8, 8>;
+    case 5: return (const void*)batch_divgroup_kernel<8, 16>;
     case 6: return (const void*)batch_divwarp_kernel<8>;
     case 7: return (const void*)batch_divwarp_kernel<16>;
     case 8: return (const void*)batch_divwarp_kernel<32>;
@@ -375,8 +406,11 @@ static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
         if (!n) continue;
         int threads = 0;
         const void* k = div_class_kernel(c, &threads);
-        // instances per CTA: one a thread, one a warp, one a CTA
-        const uint64_t per = c < DIV_THREAD_CLASSES ? (uint64_t)threads : c < DIV_CTA_CLASS ? (uint64_t)threads / 32 : 1;
+        // instances per CTA: one a thread, one a lane group (8, 16 or 32 lanes), one a CTA
+        static constexpr uint32_t group_ipw[DIV_WARP_CLASSES] = {4, 4, 2, 1, 1, 1};
+        const uint64_t per = c < DIV_THREAD_CLASSES ? (uint64_t)threads
+                             : c < DIV_CTA_CLASS    ? (uint64_t)threads / 32 * group_ipw[c - DIV_THREAD_CLASSES]
+                                                    : 1;
         BI_RETURN_IF(grid_for(k, threads, L->smem[2 + c], (n + per - 1) / per, sms, &L->grid[2 + c]));
     }
     return BI_OK;
@@ -417,9 +451,9 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
             case 0: batch_divthread_kernel<4><<<grid, DIV_THREAD_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 1: batch_divthread_kernel<8><<<grid, DIV_THREAD_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 2: batch_divthread_kernel<16><<<grid, DIV_THREAD_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
-            case 3: batch_divwarp_kernel<1><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
-            case 4: batch_divwarp_kernel<2><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
-            case 5: batch_divwarp_kernel<4><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 3: batch_divgroup_kernel<4, 8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 4: batch_divgroup_kernel<8, 8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 5: batch_divgroup_kernel<8, 16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 6: batch_divwarp_kernel<8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 7: batch_divwarp_kernel<16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 8: batch_divwarp_kernel<32><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;

@@ -131,19 +131,51 @@ div_warp_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict_
     }
 }
 
+// Several instances a warp: long division on G-lane groups (divsmall.cuh).
+template <typename T, int VPL, int G>
+__global__ void __launch_bounds__(DIV_WARP_CTA)
+div_group_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
+                 uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
+    constexpr uint32_t ipw = 32 / G;
+    const uint32_t MU = sizeof(T) == 8 ? mu : (mu + 1) / 2, MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    const uint64_t warps = (uint64_t)gridDim.x * (DIV_WARP_CTA / 32);
+    for (uint64_t w = (uint64_t)blockIdx.x * (DIV_WARP_CTA / 32) + threadIdx.x / 32; w * ipw < n; w += warps) {
+        const uint64_t inst = w * ipw + (threadIdx.x & 31) / G;
+        const bool valid = inst < n;
+        const uint64_t k = valid ? inst : 0;   // an invalid group reads and writes nothing
+        const T* ui = u + k * mu;
+        const T* vi = v + k * mv;
+        T* qi = q + k * mu;
+        T* ri = r + k * mv;
+        const uint8_t st = div_group<VPL, G>(
+            valid, MU, MV, [&](uint32_t i) { return limb64(ui, mu, i); }, [&](uint32_t i) { return limb64(vi, mv, i); },
+            [&](uint32_t i, uint64_t x) { put_limb64(qi, mu, i, x); },
+            [&](uint32_t i, uint64_t x) { put_limb64(ri, mv, i, x); });
+        if (status && valid && (threadIdx.x & (G - 1)) == 0) status[inst] = st;
+    }
+}
+
+// Long division for divisors of 17..1024 64-bit limbs: the group shape per
+// divisor size that ran fastest on GB300 (2m/m divisions, thousands of
+// instances): 8-lane groups of 4 and 8 limbs a lane up to 32 and 64 limbs,
+// 16-lane groups of 8 up to 128, a whole warp of 8 up to 256, 16-lane groups
+// of 32 up to 512, a warp of 32 up to 1024.
 template <typename T>
 static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
                             uint64_t n, cudaStream_t s) {
     const uint32_t MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
-    constexpr uint32_t per_cta = DIV_WARP_CTA / 32;
-    const uint64_t blocks = (n + per_cta - 1) / per_cta;
-    const unsigned grid = (unsigned)(blocks < (1u << 20) ? blocks : (1u << 20));
-    if (MV <= 32) div_warp_kernel<T, 1><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
-    else if (MV <= 64) div_warp_kernel<T, 2><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
-    else if (MV <= 128) div_warp_kernel<T, 4><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
-    else if (MV <= 256) div_warp_kernel<T, 8><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
-    else if (MV <= 512) div_warp_kernel<T, 16><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
-    else div_warp_kernel<T, 32><<<grid, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    constexpr uint32_t WPC = DIV_WARP_CTA / 32;   // warps per CTA
+    auto grid_for = [&](uint32_t ipw) {
+        const uint64_t warps = (n + ipw - 1) / ipw;
+        const uint64_t blocks = (warps + WPC - 1) / WPC;
+        return (unsigned)(blocks < (1u << 20) ? blocks : (1u << 20));
+    };
+    if (MV <= 32) div_group_kernel<T, 4, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 64) div_group_kernel<T, 8, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 128) div_group_kernel<T, 8, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 256) div_warp_kernel<T, 8><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 512) div_group_kernel<T, 32, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else div_warp_kernel<T, 32><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
 }
 
 constexpr uint32_t DIV_MAX_MU64 = 2048;

@@ -375,4 +375,234 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
     return 0;
 }
 
+// Carry (or borrow) into this lane of a chain over a G-lane group (lanes
+// gbase .. gbase + G - 1 of the warp), as warp_chain_in; cout = out of the
+// group's top lane.  Every lane of the warp calls it.
+template <int G>
+__device__ __forceinline__ uint64_t group_chain_in(bool g, bool p, uint64_t& cout) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gbase = lane & ~(uint32_t)(G - 1), r = lane & (G - 1);
+    const uint32_t Aw = __ballot_sync(0xffffffffu, g || p), Bw = __ballot_sync(0xffffffffu, g);
+    const uint64_t gm = G == 32 ? 0xffffffffull : ((1ull << G) - 1);
+    const uint64_t A = (Aw >> gbase) & gm, B = (Bw >> gbase) & gm;
+    const uint64_t s = A + B;
+    cout = (s >> G) & 1u;
+    return ((s ^ A ^ B) >> r) & 1u;
+}
+
+// div_warp on a G-lane group (G = 8, 16 or 32), 32 / G instances a warp: the
+// steps of a quotient limb whose cost does not grow with the divisor -- the
+// estimate, the ballots, the shuffles, the slide -- are shared by the warp's
+// instances, so small and medium divisors (where they are most of the work)
+// divide several times faster per instance.  All 32 lanes call it; each
+// group passes its own instance (valid = false: no instance, nothing read or
+// written).  Loops whose trip count differs between groups run to the warp's
+// maximum with the work of the finished (or not yet started) groups masked:
+// the quotient loop is aligned at its end, a group's first quotient limb
+// waiting for the warp's longest; a group that is not yet active uses
+// q-hat = 0, which leaves its window as it is.  Returns the status as
+// div_warp does.
+template <int VPL, int G, typename LoadU, typename LoadV, typename StoreQ, typename StoreR>
+__device__ __forceinline__ uint8_t div_group(bool valid, uint32_t MU, uint32_t MV, LoadU load_u, LoadV load_v,
+                                             StoreQ store_q, StoreR store_r) {
+    static_assert(G == 8 || G == 16 || G == 32, "div_group: G is 8, 16 or 32");
+    constexpr int MX = G * VPL;
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = (int)(threadIdx.x & 31);
+    const int r = lane & (G - 1);
+    const uint32_t gbase = (uint32_t)(lane & ~(G - 1));
+    const uint32_t gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+    uint64_t D[VPL];
+#pragma unroll
+    for (int i = 0; i < VPL; i++) {
+        const int idx = r * VPL + i - (MX - (int)MV);
+        D[i] = (valid && idx >= 0) ? load_v((uint32_t)idx) : 0;
+    }
+    int top_i = -1;
+#pragma unroll
+    for (int i = 0; i < VPL; i++)
+        if (D[i] != 0) top_i = i;
+    const uint32_t nz = __ballot_sync(FULL, top_i >= 0) & gmask;
+    const bool zero = nz == 0;                       // a zero divisor, or no instance
+    const int tl = zero ? 0 : 31 - __clz((int)nz) - (int)gbase;
+    const int ti = __shfl_sync(FULL, top_i, tl, G);
+    const int ptop = zero ? MX - 1 : tl * VPL + ti;  // top nonzero position
+    const int K = zero ? (int)MU + 1 : ptop - (MX - (int)MV) + 1;
+    const int zl = zero ? 0 : MX - K;
+    {
+        const int nsh = MX - 1 - ptop;               // one-limb shifts up
+        const int nsh_max = (int)__reduce_max_sync(FULL, (unsigned)nsh);
+        for (int z = 0; z < nsh_max; z++) {
+            const uint64_t from_below = __shfl_up_sync(FULL, D[VPL - 1], 1, G);
+            if (z < nsh) {
+#pragma unroll
+                for (int i = VPL - 1; i > 0; i--) D[i] = D[i - 1];
+                D[0] = r == 0 ? 0 : from_below;
+            }
+        }
+    }
+    const uint64_t dtop = __shfl_sync(FULL, D[VPL - 1], G - 1, G);
+    const int s = zero ? 0 : __clzll((long long)dtop);
+    const int rs = 63 - s;   // x >> (64 - s) written as (x >> 1) >> rs: 0 when s == 0
+    {
+        const uint64_t below = __shfl_up_sync(FULL, D[VPL - 1], 1, G);
+        uint64_t prev = r == 0 ? 0 : below;
+#pragma unroll
+        for (int i = 0; i < VPL; i++) {
+            const uint64_t cur = D[i];
+            D[i] = (cur << s) | ((prev >> 1) >> rs);
+            prev = cur;
+        }
+    }
+    const uint64_t d1 = __shfl_sync(FULL, D[VPL - 1], G - 1, G);
+    const uint64_t d2 = VPL >= 2 ? __shfl_sync(FULL, D[VPL >= 2 ? VPL - 2 : 0], G - 1, G)
+                                 : __shfl_sync(FULL, D[0], G - 2, G);
+    const uint64_t vr = recip_limb(zero ? (1ull << 63) : d1);
+
+    auto raw = [&](int t) -> uint64_t { return (valid && t >= 0 && t < (int)MU) ? load_u((uint32_t)t) : 0; };
+    auto sh = [&](int t) -> uint64_t { return (raw(t) << s) | ((raw(t - 1) >> 1) >> rs); };
+    uint64_t R[VPL];
+    {
+        const int t0 = (int)MU - MX + r * VPL;
+        uint64_t prev = raw(t0 - 1);
+#pragma unroll
+        for (int i = 0; i < VPL; i++) {
+            const uint64_t cur = raw(t0 + i);
+            R[i] = (cur << s) | ((prev >> 1) >> rs);
+            prev = cur;
+        }
+    }
+    uint64_t rtop = (raw((int)MU - 1) >> 1) >> rs;
+    int base = (int)MU - MX - 1, c = 0;   // stream buffer: rank r holds sh(base - r)
+    uint64_t shb = sh(base - r);
+    const int nsteps = zero ? 0 : (int)MU - K + 1;
+    const int nmax = (int)__reduce_max_sync(FULL, (unsigned)nsteps);
+    for (int j = nmax - 1; j >= 0; j--) {            // this group's quotient limb j while j < nsteps
+        const bool act = j < nsteps;
+        const uint64_t u2 = rtop;
+        const uint64_t u1 = __shfl_sync(FULL, R[VPL - 1], G - 1, G);
+        const uint64_t u0 = VPL >= 2 ? __shfl_sync(FULL, R[VPL >= 2 ? VPL - 2 : 0], G - 1, G)
+                                     : __shfl_sync(FULL, R[0], G - 2, G);
+        uint64_t qh = 0, rh = 0;
+        if (act) {
+            bool rh_over = false;
+            if (u2 >= d1) {                          // u2 == d1: q-hat = B - 1, r-hat = u1 + d1
+                qh = ~0ull;
+                rh = u1 + d1;
+                rh_over = rh < u1;
+            } else {
+                qh = div_2by1(u2, u1, d1, vr, rh);
+            }
+            for (int t = 0; t < 2 && !rh_over; t++) {   // q-hat * d2 > r-hat * B + u0: one too large
+                const uint64_t p_lo = qh * d2, p_hi = __umul64hi(qh, d2);
+                if (p_hi > rh || (p_hi == rh && p_lo > u0)) {
+                    qh -= 1;
+                    const uint64_t nr = rh + d1;
+                    rh_over = nr < rh;
+                    rh = nr;
+                } else {
+                    break;
+                }
+            }
+        }
+        // R -= q-hat D in two passes as div_warp (q-hat = 0 leaves R as it is)
+        uint64_t coutA, coutB;
+        bool neg;
+        {
+            const uint64_t htop = __umul64hi(qh, D[VPL - 1]);
+            const uint64_t hb = __shfl_up_sync(FULL, htop, 1, G);
+            const uint64_t h0 = r == 0 ? 0 : hb;
+            const uint32_t gA = chain_sub_from<VPL>(
+                R, [&](int i) { return i == 0 ? h0 : __umul64hi(qh, D[i > 0 ? i - 1 : 0]); }, 0);
+            uint64_t orA = 0;
+#pragma unroll
+            for (int i = 0; i < VPL; i++) orA |= R[i];
+            const bool zA = orA == 0;
+            const uint32_t binA = (uint32_t)group_chain_in<G>(gA != 0, zA, coutA);
+            const uint64_t th = __shfl_sync(FULL, htop, G - 1, G);
+            const uint64_t x = rtop - th;
+            const bool bA = (rtop < th) || (x < coutA);
+            rtop = x - coutA;
+            const uint32_t gB = chain_sub_from<VPL>(R, [&](int i) { return qh * D[i]; }, binA) &
+                                (zA && binA ? 0u : 1u);
+            uint64_t orB = 0;
+#pragma unroll
+            for (int i = 0; i < VPL; i++) orB |= R[i];
+            const bool zB = orB == 0;
+            const uint32_t bin = (uint32_t)group_chain_in<G>(gB != 0, zB, coutB);
+            chain_sub_from<VPL>(R, [](int) { return 0ull; }, bin);
+            const bool bB = rtop < coutB;
+            rtop -= coutB;
+            neg = bA || bB;
+        }
+        if (__any_sync(FULL, neg)) {                 // rare: add D back where q-hat was one too large
+            if (neg) qh -= 1;
+            uint64_t cy = 0;
+            bool allo = true;
+#pragma unroll
+            for (int i = 0; i < VPL; i++) {
+                const uint64_t di = neg ? D[i] : 0;
+                const uint64_t x = R[i] + di;
+                const uint64_t c1 = x < di ? 1 : 0;
+                const uint64_t y = x + cy;
+                cy = c1 | (y < x ? 1 : 0);
+                R[i] = y;
+                allo &= y == ~0ull;
+            }
+            uint64_t cout;
+            uint64_t cin = group_chain_in<G>(cy != 0, allo && neg, cout);
+#pragma unroll
+            for (int i = 0; i < VPL; i++) {
+                const uint64_t y = R[i];
+                R[i] = y + cin;
+                cin &= y == ~0ull ? 1 : 0;
+            }
+            rtop += cout;
+        }
+        if (act && r == 0) store_q((uint32_t)j, qh);
+        if (j > 0) {                                 // slide the window down one limb (active groups)
+            const uint64_t next = __shfl_sync(FULL, shb, c, G);
+            const uint64_t newtop = __shfl_sync(FULL, R[VPL - 1], G - 1, G);
+            const uint64_t from_below = __shfl_up_sync(FULL, R[VPL - 1], 1, G);
+            if (act) {
+                rtop = newtop;
+#pragma unroll
+                for (int i = VPL - 1; i > 0; i--) R[i] = R[i - 1];
+                R[0] = r == 0 ? next : from_below;
+                if (++c == G) {
+                    base -= G;
+                    c = 0;
+                    shb = sh(base - r);
+                }
+            }
+        }
+    }
+    if (valid)
+        for (uint32_t i = (uint32_t)((int)MU - K + 1) + (uint32_t)r; i < MU; i += G) store_q(i, 0);
+    // remainder: positions 0..MX-1 hold (r 2^s) B^zl
+    {
+        const int zl_max = (int)__reduce_max_sync(FULL, (unsigned)zl);
+        for (int z = 0; z < zl_max; z++) {
+            const uint64_t from_above = __shfl_down_sync(FULL, R[0], 1, G);
+            if (z < zl) {
+#pragma unroll
+                for (int i = 0; i < VPL - 1; i++) R[i] = R[i + 1];
+                R[VPL - 1] = r == G - 1 ? 0 : from_above;
+            }
+        }
+    }
+    {
+        const uint64_t ab = __shfl_down_sync(FULL, R[0], 1, G);
+        const uint64_t above = r == G - 1 ? 0 : ab;
+#pragma unroll
+        for (int i = 0; i < VPL; i++) {
+            const uint64_t hi = i + 1 < VPL ? R[i + 1 < VPL ? i + 1 : 0] : above;
+            const uint64_t x = zero ? 0 : (R[i] >> s) | ((hi << 1) << rs);
+            const int p = r * VPL + i;
+            if (valid && p < (int)MV) store_r((uint32_t)p, x);
+        }
+    }
+    return zero ? 1 : 0;
+}
+
 }  // namespace bi
