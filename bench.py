@@ -28,7 +28,7 @@ Multi-GPU: instances are independent, so N ranks run N replicas of the step
 (weak scaling, no collective on the data path; NCCL only carries the barrier
 and the max over ranks of the elapsed time).
 
-`--workload add|sub|mul|mul2048|div|batch|serve` with `--bits`, `--total-limbs-log2`,
+`--workload add|sub|mul|mul2048|div|divsweep|batch|serve` with `--bits`, `--total-limbs-log2`,
 `--mul-m`, `--div-m`, `--batch-n` runs one operation on one size, or the
 uneven batch, alone (used for profiling).
 """
@@ -288,14 +288,15 @@ def run_reference(args) -> None:
 
 def div_method(mv: int, n: int, sms: int) -> str:
     """The method bi_div_u64 picks for n divisions by mv-limb divisors
-    (div_use_long in divsmall.cuh): long division on one thread or one warp
-    per instance, or the shifted inverse on one CTA per instance."""
+    (div_use_long in divsmall.cuh): long division on one thread or one lane
+    group (8, 16 or 32 lanes) per instance, or the shifted inverse on one CTA
+    per instance."""
     if mv <= 16:
         return "long_thread"
-    if mv <= 128:
-        return "long_warp"
-    if mv <= 1024 and n > (2 if mv <= 256 else 3 if mv <= 512 else 6) * sms:
-        return "long_warp"
+    if mv <= 32:
+        return "long_group"
+    if mv <= 1024 and n > (5 if mv <= 64 else 3 if mv <= 256 else 6) * sms:
+        return "long_group"
     return "shinv"
 
 
@@ -712,6 +713,25 @@ def run_single(args) -> None:
                                                     st.data_ptr(), 2 * mv, mv, n, sp)), args.steps, args.warmup)
         print(json.dumps({"workload": w, "m": mv, "n": n, "method": args.div_method, "ms": ms,
                           "instances_per_s": n / ms * 1e3}))
+    elif w == "divsweep":
+        # long division vs the shifted inverse over divisor sizes and batch sizes (2m/m)
+        rows = {}
+        for mv in (32, 64, 128, 256, 512, 1024):
+            mu = 2 * mv
+            for n in (1, 38, 152, 304, 608, 1216, 2432):
+                u = device_uniform_u64(11, n, mu)
+                v = device_uniform_u64(12, n, mv)
+                v[:, -1] |= 1
+                q, rr = torch.empty_like(u), torch.empty_like(v)
+                st = torch.empty(n, dtype=torch.uint8, device="cuda")
+                row = {}
+                for name in ("bi_div_long_u64", "bi_div_shinv_u64"):
+                    fn = getattr(L, name)
+                    ms = event_time(stream, lambda: check(L, fn(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
+                                                                st.data_ptr(), mu, mv, n, sp)), 5 if mv < 512 else 2)
+                    row[name] = round(ms * 1e3, 1)
+                rows[f"{mu}/{mv} n={n}"] = {"long_us": row["bi_div_long_u64"], "shinv_us": row["bi_div_shinv_u64"]}
+        print(json.dumps({"workload": w, "us_per_call": rows}))
     elif w == "mul2048":
         from bigint_gb300.workloads import mul2048_u32
 
@@ -930,7 +950,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="addsub",
-                    choices=["addsub", "add", "sub", "mul", "mul2048", "div", "batch", "serve"])
+                    choices=["addsub", "add", "sub", "mul", "mul2048", "div", "divsweep", "batch", "serve"])
     ap.add_argument("--bits", type=int, default=0, help="restrict the add/sub sweep to one size")
     ap.add_argument("--total-limbs-log2", type=int, default=27)
     ap.add_argument("--mul-m", type=int, default=1024)

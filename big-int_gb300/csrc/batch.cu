@@ -311,9 +311,13 @@ static size_t mul_smem_for(const bi_plan* p, int ipc_div) {
 }
 
 // The class of each division: by divisor size (div_class), except that a
-// warp class with too few divisions for long division's throughput to win
-// (div_use_long, the same measured crossover as a uniform batch) goes to the
-// shifted inverse on CTAs.  map[c] is the class that size class c runs as.
+// class above 128 limbs with too few divisions for long division's
+// throughput to win goes to the shifted inverse on CTAs: at most 2, 3 and 6
+// per SM for divisors up to 256, 512 and 1024 limbs.  (Up to 128 limbs long
+// division stays: beside the batch's other kernels its small lane groups
+// pack where a CTA per division does not -- a 20000-instance batch ran
+// 1.74 ms so and 1.94 ms with the uniform entry's crossover.)  map[c] is the
+// class that size class c runs as.
 static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n, int sms, int* map) {
     uint64_t cnt[DIV_CLASSES] = {};
     for (uint32_t k = 0; k < n; k++) cnt[div_class(descs[div[k]].mb)]++;
@@ -321,7 +325,10 @@ static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n,
         map[c] = c;
         if (c >= DIV_THREAD_CLASSES && c < DIV_CTA_CLASS) {
             const uint32_t max_mv = 32u << (c - DIV_THREAD_CLASSES);   // the class's largest divisor
-            if (!div_use_long(max_mv, cnt[c], sms)) map[c] = DIV_CTA_CLASS;
+            if (max_mv > 128) {
+                const uint64_t per_sm = max_mv <= 256 ? 2 : max_mv <= 512 ? 3 : 6;
+                if (cnt[c] <= per_sm * (uint64_t)sms) map[c] = DIV_CTA_CLASS;
+            }
         }
     }
 }

@@ -25,18 +25,19 @@ constexpr int DIV_THREAD_MAX_MV = 16;   // 64-bit divisor limbs handled by div_t
 constexpr int DIV_THREAD_CTA = 64;      // threads per CTA of the one-thread-per-instance kernels
 constexpr int DIV_WARP_MAX_MV = 1024;   // 64-bit divisor limbs handled by div_warp
 constexpr int DIV_WARP_CTA = 128;       // threads per CTA of the one-warp-per-instance kernels
-// Long division on warps or the shifted inverse on CTAs, for a batch of n
-// instances with MV-limb divisors (64-bit limbs) on a GPU of `sms` SMs.
+// Long division on lane groups or the shifted inverse on CTAs, for a batch
+// of n instances with MV-limb divisors (64-bit limbs) on a GPU of `sms` SMs.
 // Long division does fewer limb products but runs one quotient limb after
-// another (about 0.5 us per limb at 64 limbs, 1.5 us at 1024), so with few
-// instances one CTA per instance finishes sooner; past a few instances per SM
-// the warps' throughput wins.  Measured crossovers (dividend 2 MV limbs,
-// GB300): long division always up to 128 limbs; above that once n exceeds
-// 2, 3 and 6 instances per SM for divisors up to 256, 512 and 1024 limbs.
+// another (0.4 to 1.5 us a limb), so with few instances one CTA per instance
+// finishes sooner; past a few instances per SM the groups' throughput wins.
+// Measured crossovers (dividend 2 MV limbs, GB300, the shapes div.cu
+// launches): long division always up to 32 limbs; above that once n exceeds
+// 5, 3, 3, 6 and 6 instances per SM for divisors up to 64, 128, 256, 512 and
+// 1024 limbs.
 __host__ __device__ inline bool div_use_long(uint32_t MV, uint64_t n, int sms) {
-    if (MV <= (uint32_t)DIV_THREAD_MAX_MV || MV <= 128) return true;
+    if (MV <= 32) return true;
     if (MV > (uint32_t)DIV_WARP_MAX_MV) return false;
-    const uint64_t per_sm = MV <= 256 ? 2 : MV <= 512 ? 3 : 6;
+    const uint64_t per_sm = MV <= 64 ? 5 : MV <= 256 ? 3 : 6;
     return n > per_sm * (uint64_t)sms;
 }
 
