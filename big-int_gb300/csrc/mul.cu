@@ -420,8 +420,9 @@ static bi_status mul_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n,
         return set_error(BI_EINVAL, "buffers must be aligned to the limb size");
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul chain: m=%u above the supported size", m);
-    const uint64_t fill = (n + 2ull * num_sms() - 1) / (2ull * num_sms());
-    MulGeom g = mul_geometry(L, false, fill < 256 ? (uint32_t)(fill ? fill : 1) : 256u);
+    MulGeom g = mul_geom_for<T, false>(L, n);   // the uniform multiply's tiling (128-thread CTAs unless tuned)
+    g.S = 1;                                     // the chain kernel does not slice rows
+    g.lgS = 0;
     g.m = m;
     g.out_words = m;
     const uint32_t threads = (g.ipc * g.tpi + 31) / 32 * 32;
