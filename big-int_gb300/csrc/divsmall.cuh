@@ -169,6 +169,23 @@ __device__ __forceinline__ uint8_t div_thread(uint32_t MU, uint32_t MV, LoadU lo
     return 0;
 }
 
+// R -= bin (0 or 1) over a lane's block: the borrow stops at R[0] unless
+// R[0] was zero, so the chain through the other limbs is a rare branch.
+template <int VPL>
+__device__ __forceinline__ void lane_borrow_in(uint64_t (&R)[VPL], uint32_t bin) {
+    const uint64_t y0 = R[0];
+    R[0] = y0 - bin;
+    if (bin && y0 == 0) {
+        uint64_t b = 1;
+#pragma unroll
+        for (int i = 1; i < VPL; i++) {
+            const uint64_t y = R[i];
+            R[i] = y - b;
+            b &= y == 0 ? 1 : 0;
+        }
+    }
+}
+
 // Borrow (or carry) into this lane of a warp-wide chain, from each lane's
 // generate g (out with nothing in) and propagate p (out only with one in):
 // bit l of (A + B) ^ A ^ B with A = ballot(g | p), B = ballot(g).  cout gets
@@ -310,7 +327,7 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
             for (int i = 0; i < VPL; i++) orB |= R[i];
             const bool zB = orB == 0;
             uint32_t bin = (uint32_t)warp_chain_in(gB != 0, zB, coutB);
-            chain_sub_from<VPL>(R, [](int) { return 0ull; }, bin);
+            lane_borrow_in<VPL>(R, bin);
             const bool bB = rtop < coutB;
             rtop -= coutB;
             neg = bA || bB;                    // at most one of the two wraps
@@ -531,7 +548,7 @@ __device__ __forceinline__ uint8_t div_group(bool valid, uint32_t MU, uint32_t M
             for (int i = 0; i < VPL; i++) orB |= R[i];
             const bool zB = orB == 0;
             const uint32_t bin = (uint32_t)group_chain_in<G>(gB != 0, zB, coutB);
-            chain_sub_from<VPL>(R, [](int) { return 0ull; }, bin);
+            lane_borrow_in<VPL>(R, bin);
             const bool bB = rtop < coutB;
             rtop -= coutB;
             neg = bA || bB;
