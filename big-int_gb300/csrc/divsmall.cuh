@@ -169,6 +169,18 @@ __device__ __forceinline__ uint8_t div_thread(uint32_t MU, uint32_t MV, LoadU lo
     return 0;
 }
 
+// The lane's block is zero (the borrow chain's propagate bit): a random block
+// almost never is, and its first and last limbs settle that; the OR of all
+// limbs only when both are zero.
+template <int VPL>
+__device__ __forceinline__ bool lane_is_zero(const uint64_t (&R)[VPL]) {
+    if ((R[0] | R[VPL - 1]) != 0) return false;
+    uint64_t o = 0;
+#pragma unroll
+    for (int i = 0; i < VPL; i++) o |= R[i];
+    return o == 0;
+}
+
 // R -= bin (0 or 1) over a lane's block: the borrow stops at R[0] unless
 // R[0] was zero, so the chain through the other limbs is a rare branch.
 template <int VPL>
@@ -308,10 +320,7 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
             const uint64_t h0 = lane == 0 ? 0 : hb;
             const uint32_t gA = chain_sub_from<VPL>(
                 R, [&](int i) { return i == 0 ? h0 : __umul64hi(qh, Dv(i > 0 ? i - 1 : 0)); }, 0);
-            uint64_t orA = 0;   // the lane's block is zero: one compare of the OR of its limbs
-#pragma unroll
-            for (int i = 0; i < VPL; i++) orA |= R[i];
-            const bool zA = orA == 0;
+            const bool zA = lane_is_zero<VPL>(R);
             const uint32_t binA = (uint32_t)warp_chain_in(gA != 0, zA, coutA);
             const uint64_t th = __shfl_sync(FULL, htop, 31);
             const uint64_t x = rtop - th;
@@ -322,10 +331,7 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
             // A's ballots already carried on, so it generates no B borrow
             const uint32_t gB = chain_sub_from<VPL>(R, [&](int i) { return qh * Dv(i); }, binA) &
                                 (zA && binA ? 0u : 1u);
-            uint64_t orB = 0;
-#pragma unroll
-            for (int i = 0; i < VPL; i++) orB |= R[i];
-            const bool zB = orB == 0;
+            const bool zB = lane_is_zero<VPL>(R);
             uint32_t bin = (uint32_t)warp_chain_in(gB != 0, zB, coutB);
             lane_borrow_in<VPL>(R, bin);
             const bool bB = rtop < coutB;
@@ -532,10 +538,7 @@ __device__ __forceinline__ uint8_t div_group(bool valid, uint32_t MU, uint32_t M
             const uint64_t h0 = r == 0 ? 0 : hb;
             const uint32_t gA = chain_sub_from<VPL>(
                 R, [&](int i) { return i == 0 ? h0 : __umul64hi(qh, D[i > 0 ? i - 1 : 0]); }, 0);
-            uint64_t orA = 0;
-#pragma unroll
-            for (int i = 0; i < VPL; i++) orA |= R[i];
-            const bool zA = orA == 0;
+            const bool zA = lane_is_zero<VPL>(R);
             const uint32_t binA = (uint32_t)group_chain_in<G>(gA != 0, zA, coutA);
             const uint64_t th = __shfl_sync(FULL, htop, G - 1, G);
             const uint64_t x = rtop - th;
@@ -543,10 +546,7 @@ __device__ __forceinline__ uint8_t div_group(bool valid, uint32_t MU, uint32_t M
             rtop = x - coutA;
             const uint32_t gB = chain_sub_from<VPL>(R, [&](int i) { return qh * D[i]; }, binA) &
                                 (zA && binA ? 0u : 1u);
-            uint64_t orB = 0;
-#pragma unroll
-            for (int i = 0; i < VPL; i++) orB |= R[i];
-            const bool zB = orB == 0;
+            const bool zB = lane_is_zero<VPL>(R);
             const uint32_t bin = (uint32_t)group_chain_in<G>(gB != 0, zB, coutB);
             lane_borrow_in<VPL>(R, bin);
             const bool bB = rtop < coutB;
