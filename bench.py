@@ -407,11 +407,13 @@ def measure_extra(B, L, stream, args):
         q = torch.empty_like(u)
         rr = torch.empty_like(v)
         st = torch.empty(n, dtype=torch.uint8, device="cuda")
-        ms = event_time(stream, lambda: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
-                                                               st.data_ptr(), 2 * mv, mv, n, sp)), 3, 1)
-        ms_shinv = event_time(stream, lambda: check(L, L.bi_div_shinv_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(),
-                                                                           rr.data_ptr(), st.data_ptr(), 2 * mv, mv, n,
-                                                                           sp)), 3, 1)
+        # one replay of a CUDA graph of the calls: the shortest divisions take ~10 us, which
+        # the host's per-call overhead would otherwise set
+        ms = graph_time(lambda s_: check(L, L.bi_div_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(), rr.data_ptr(),
+                                                           st.data_ptr(), 2 * mv, mv, n, s_)), 5)
+        ms_shinv = graph_time(lambda s_: check(L, L.bi_div_shinv_u64(u.data_ptr(), v.data_ptr(), q.data_ptr(),
+                                                                       rr.data_ptr(), st.data_ptr(), 2 * mv, mv, n,
+                                                                       s_)), 5)
         method = div_method(mv, n, torch.cuda.get_device_properties(0).multi_processor_count)
         # 32x32-bit word products per division of the method that ran
         wp = 4 * (div_limb_products(2 * mv, mv) if method == "shinv" else long_div_limb_products(2 * mv, mv))

@@ -113,24 +113,16 @@ __device__ __forceinline__ uint8_t div_thread(uint32_t MU, uint32_t MV, LoadU lo
                 break;
             }
         }
-        // R -= q-hat * D
-        uint64_t carry = 0, borrow = 0;
-#pragma unroll
-        for (int k = 0; k < MX; k++) {
-            const uint64_t plo = qh * D[k], phi = __umul64hi(qh, D[k]);
-            const uint64_t sub = plo + carry;
-            carry = phi + (sub < plo ? 1 : 0);
-            const uint64_t y = R[k] - sub;
-            const uint64_t b1 = R[k] < sub ? 1 : 0;
-            R[k] = y - borrow;
-            borrow = b1 | (y < borrow ? 1 : 0);
-        }
-        {
-            const uint64_t y = R[MX] - carry;
-            const uint64_t b1 = R[MX] < carry ? 1 : 0;
-            R[MX] = y - borrow;
-            borrow = b1 | (y < borrow ? 1 : 0);
-        }
+        // R -= q-hat * D on the carry flag: the high halves one limb up (R[1..MX]),
+        // then the low halves (R[0..MX-1], the borrow out taken from R[MX]);
+        // the result is negative iff one of the two wrapped
+        const uint32_t bA = chain_sub_from<MX>(*reinterpret_cast<uint64_t(*)[MX]>(&R[1]),
+                                               [&](int k) { return __umul64hi(qh, D[k]); }, 0);
+        const uint32_t bo = chain_sub_from<MX>(*reinterpret_cast<uint64_t(*)[MX]>(&R[0]),
+                                               [&](int k) { return qh * D[k]; }, 0);
+        const bool bB = R[MX] < bo;
+        R[MX] -= bo;
+        const bool borrow = bA != 0 || bB;
         if (borrow) {                          // one too large after all: add D back
             qh -= 1;
             uint64_t c = 0;
