@@ -23,9 +23,15 @@ struct DivGeom {
     uint32_t smem_limbs;
 };
 
-// The first iterate of the shifted inverse comes from long division up to
-// this precision (limbs; div_warp<2> holds divisors up to 64 limbs).
-constexpr int DIV_INIT_LONG_MAX = 64;
+// The first iterate of the shifted inverse comes from long division: the
+// whole inverse when its precision is at most DIV_INIT_LONG_ALL limbs (no
+// Newton step at all; div_warp<2> holds divisors up to 64 limbs), else up to
+// DIV_INIT_LONG_MAX limbs -- on one warp a quotient limb costs about 800
+// cycles and a Newton step on the CTA 13-18K at these precisions, so long
+// division to 32 limbs and one more step beat long division to 64 (512/256
+// limbs: 167K -> 163K cycles; 1024/512: 334K -> 326K).
+constexpr int DIV_INIT_LONG_ALL = 64;
+constexpr int DIV_INIT_LONG_MAX = 32;
 
 // One Newton step of the shifted inverse, from precision p to pn: Y_p (p + 1
 // limbs at Yb + (Pmax - p)) becomes Y_pn (pn + 1 limbs at Yb + (Pmax - pn)).
@@ -117,14 +123,15 @@ __device__ __forceinline__ void div_cta(const DivGeom& g, uint64_t* smem, LoadU 
             sched[ns++] = x;
         }
     }
-    // start at p0, the largest scheduled precision <= DIV_INIT_LONG_MAX:
-    // Y_p0 = floor((B^(2 p0) - 1) / D) for D = the top p0 limbs of v, by long
-    // division on one warp (divsmall.cuh) -- about p0 quotient limbs of a few
-    // hundred cycles each, where the Newton steps it replaces cost a block
-    // product and barriers each
+    // start at p0 -- P itself when P <= DIV_INIT_LONG_ALL, else the largest
+    // scheduled precision <= DIV_INIT_LONG_MAX: Y_p0 = floor((B^(2 p0) - 1) / D)
+    // for D = the top p0 limbs of v, by long division on one warp
+    // (divsmall.cuh) -- about p0 quotient limbs of a few hundred cycles each,
+    // where the Newton steps it replaces cost a block product and barriers each
     int p0 = 2;
+    const int init_cap = P <= DIV_INIT_LONG_ALL ? P : DIV_INIT_LONG_MAX;
     for (int si = 0; si < ns; si++)
-        if (sched[si] <= DIV_INIT_LONG_MAX && sched[si] > p0) p0 = sched[si];
+        if (sched[si] <= init_cap && sched[si] > p0) p0 = sched[si];
     const bool init_warp = std::is_same<Grp, CtaGroup>::value ? threadIdx.x < 32 : true;
     if (init_warp) {
         auto ld_u = [](uint32_t) { return ~0ull; };
