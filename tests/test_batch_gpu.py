@@ -184,6 +184,47 @@ def test_batch_matches_per_size_kernels(bigint):
     torch.cuda.synchronize()
 
 
+def test_full_size_batch_matches_per_size_kernels(bigint):
+    """The benchmark's batch itself (100000 instances, 256..65536 bits, the
+    mix and seed of the uneven-batch workload): every instance equals the
+    plain per-size kernels' result, and a sample of the divisions satisfies
+    u = q v + r with r < v in Python integers."""
+    import torch
+
+    B = bigint
+    d, arena, out_limbs, nflags = B.workloads.uneven_batch()
+    plan, din, dout, dfl = _run(B, d, arena, out_limbs, nflags)
+    out = B.to_host(dout, np.uint64)
+
+    def rows(src, off, idx, width):
+        return src[d[off][idx].astype(np.int64)[:, None] + np.arange(width)]
+
+    checked_div = 0
+    for (op, m, mb), idx in _groups(d).items():
+        idx = np.array(idx)
+        a, b = rows(arena, "a", idx, m), rows(arena, "b", idx, mb)
+        da, db = B.to_device(a), B.to_device(b)
+        if op == B.OP_ADD:
+            assert (rows(out, "r", idx, m) == B.to_host(B.add(da, db), np.uint64)).all(), ("add", m)
+        elif op == B.OP_SUB:
+            assert (rows(out, "r", idx, m) == B.to_host(B.sub(da, db)[0], np.uint64)).all(), ("sub", m)
+        elif op == B.OP_MULFULL:
+            assert (rows(out, "r", idx, 2 * m) == B.to_host(B.mulfull(da, db), np.uint64)).all(), ("mulfull", m)
+        else:
+            q, r, _ = B.div(da, db)
+            gq, gr = rows(out, "r", idx, m), rows(out, "r2", idx, mb)
+            assert (gq == B.to_host(q, np.uint64)).all() and (gr == B.to_host(r, np.uint64)).all(), ("div", m)
+            if checked_div < 200:
+                k = 0
+                to_int = lambda limbs: sum(int(x) << (64 * i) for i, x in enumerate(limbs))
+                U, V, Q, R = to_int(a[k]), to_int(b[k]), to_int(gq[k]), to_int(gr[k])
+                assert U == Q * V + R and R < V, ("div identity", m, mb)
+                checked_div += 1
+    assert checked_div > 50
+    plan.close()
+    torch.cuda.synchronize()
+
+
 def test_invalid_descriptors_rejected(bigint):
     B = bigint
     d = np.zeros(1, dtype=B.DESC_DTYPE)
