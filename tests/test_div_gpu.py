@@ -214,3 +214,34 @@ def test_exact_where_reference_prototype_is_one_short(bigint, oracle):
     assert sum(int(x) << (32 * i) for i, x in enumerate(rv)) == U % V
     qf, _, _ = oracle.div_ref(u, np.array([[*v[0], 0, 0]], np.uint32))
     assert sum(int(x) << (32 * i) for i, x in enumerate(qf[0])) == U // V - 1
+
+
+@pytest.mark.parametrize("mv,n", [(4, 1 << 16), (16, 1 << 14), (64, 1 << 13), (256, 1 << 12), (1024, 1 << 10)])
+def test_full_size_division_identity(bigint, mv, n):
+    """The benchmark's division workloads at full size (2m/m limbs, u64),
+    checked on every row by a property the division kernels do not share:
+    q v has no limbs above 2m, u - q v = r with no borrow (so u = q v + r
+    exactly), and r - v borrows (r < v) -- with the multiply and add/sub
+    kernels."""
+    import torch
+
+    B = bigint
+    from bigint_gb300.workloads import device_uniform_u64
+
+    m2 = 2 * mv
+    u = device_uniform_u64(11, n, m2)
+    v = device_uniform_u64(12, n, mv)
+    v[:, -1] |= 1
+    q, r, st = B.div(u, v)
+    assert (st == 0).all()
+    vpad = torch.zeros((n, m2), dtype=torch.int64, device="cuda")
+    vpad[:, :mv] = v
+    qv = B.mulfull(q, vpad)                       # 4m limbs
+    assert (qv[:, m2:] == 0).all()
+    diff, borrow = B.sub(u, qv[:, :m2].contiguous())
+    assert (borrow == 0).all()
+    rpad = torch.zeros((n, m2), dtype=torch.int64, device="cuda")
+    rpad[:, :mv] = r
+    assert torch.equal(diff, rpad)
+    _, lt = B.sub(r, v)
+    assert (lt == 1).all()
