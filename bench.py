@@ -239,6 +239,19 @@ def cpu_addsub(op: str, a: np.ndarray, b: np.ndarray, nthreads: int) -> float:
     return time.perf_counter() - t0
 
 
+# Samples of the multiply and division workloads for the CPU timing beside
+# them (a bounded slice of each GPU workload, about 0.1-0.4 s on 16 cores).
+CPU_MUL_SAMPLE = {64: 32768, 256: 4096, 1024: 256, 2048: 64}
+CPU_DIV_SAMPLE = {4: 65536, 16: 16384, 64: 2048, 256: 128, 1024: 8}
+
+
+def cpu_sample_rate(fn, n: int) -> float:
+    """Instances/s of fn() over n instances on the host (oracle port)."""
+    t0 = time.perf_counter()
+    fn()
+    return n / (time.perf_counter() - t0)
+
+
 # ---------------------------------------------------------------------------
 # reference arm: the reference's CPU implementation (oracle port), host cores
 # ---------------------------------------------------------------------------
@@ -368,7 +381,18 @@ def measure_extra(B, L, stream, args):
         ms_tuned = event_time(stream, lambda: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n,
                                                                          sp)), 5)
         check(L, L.bi_mul_set_tuning_u64(m, 1, 0, 0))       # back to the library's own choice
-        mul[f"m{m}_n{n}"] = {"full_instances_per_s": round(n / ms * 1e3), "full_ms": round(ms, 4),
+        cpu = None
+        if not args.no_cpu:
+            sys.path.insert(0, os.path.join(REPO, "oracle"))
+            import oracle as O
+
+            k = CPU_MUL_SAMPLE.get(m, 64)
+            ha, hb = B.to_host(a[:k], np.uint64), B.to_host(b[:k], np.uint64)
+            th = os.cpu_count() or 1
+            cpu = {"instances_per_s": round(cpu_sample_rate(lambda: O.mulfull(ha, hb, nthreads=th), k)),
+                   "threads": th, "sample": f"the first {k} pairs", "kind": "port",
+                   "what": "the oracle's C schoolbook full product (stands in for the reference's mult.c prototype)"}
+        mul[f"m{m}_n{n}"] = {"full_instances_per_s": round(n / ms * 1e3), "full_ms": round(ms, 4), "cpu": cpu,
                              "word_products_per_s": wp / ms * 1e3, "frac_of_intpipe_peak": round(wp / ms * 1e3 / peak_wps, 4),
                              "truncated_instances_per_s": round(n / ms_t * 1e3), "truncated_ms": round(ms_t, 4),
                              "autotuned_full_instances_per_s": round(n / ms_tuned * 1e3),
@@ -417,7 +441,20 @@ def measure_extra(B, L, stream, args):
         method = div_method(mv, n, torch.cuda.get_device_properties(0).multi_processor_count)
         # 32x32-bit word products per division of the method that ran
         wp = 4 * (div_limb_products(2 * mv, mv) if method == "shinv" else long_div_limb_products(2 * mv, mv))
-        div[f"m{mv}_n{n}"] = {"method": method, "instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4),
+        cpu = None
+        if not args.no_cpu:
+            sys.path.insert(0, os.path.join(REPO, "oracle"))
+            import oracle as O
+
+            k = CPU_DIV_SAMPLE.get(mv, 8)
+            hu = B.to_host(u[:k], np.uint64).view(np.uint32)
+            hv = np.zeros((k, 4 * mv), np.uint32)       # div.c divides equal sizes: v zero-extended
+            hv[:, : 2 * mv] = B.to_host(v[:k], np.uint64).view(np.uint32)
+            th = os.cpu_count() or 1
+            cpu = {"instances_per_s": round(cpu_sample_rate(lambda: O.div_ref(hu, hv, nthreads=th), k)),
+                   "threads": th, "sample": f"the first {k} pairs", "kind": "port",
+                   "what": "the oracle's restatement of prototypes/div.c div_shinv (u32 digits), all host threads"}
+        div[f"m{mv}_n{n}"] = {"method": method, "instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4), "cpu": cpu,
                               "word_products_per_div": wp, "word_products_per_s": wp * n / ms * 1e3,
                               "frac_of_intpipe_peak": round(wp * n / ms * 1e3 / peak_wps, 4),
                               "shinv_instances_per_s": round(n / ms_shinv * 1e3)}
