@@ -313,6 +313,14 @@ def div_method(mv: int, n: int, sms: int) -> str:
     return "shinv"
 
 
+def gu32ops(n: int, words: int, ms: float) -> float:
+    """The reference's own multiply rate, "Gu32ops" (cuda/main.cu:393-400):
+    300 M log2(M) u32 operations per instance of an M-word (u32) product,
+    FFT-normalised (a count for comparison with FFT multiplies, not work
+    done), in Gops/s.  M is the product's size in u32 words."""
+    return n * 300 * words * (words.bit_length() - 1) / (ms * 1e6)
+
+
 def long_div_limb_products(mu: int, mv: int) -> int:
     """64x64-bit limb products of schoolbook long division of a mu-limb
     dividend by an mv-limb divisor with a nonzero top limb: one q-hat * v row
@@ -394,7 +402,11 @@ def measure_extra(B, L, stream, args):
                    "what": "the oracle's C schoolbook full product (stands in for the reference's mult.c prototype)"}
         mul[f"m{m}_n{n}"] = {"full_instances_per_s": round(n / ms * 1e3), "full_ms": round(ms, 4), "cpu": cpu,
                              "word_products_per_s": wp / ms * 1e3, "frac_of_intpipe_peak": round(wp / ms * 1e3 / peak_wps, 4),
+                             # the reference's FFT-normalised figure: its full product is a 2m-limb
+                             # (4m-word) truncated launch on zero-padded operands
+                             "full_gu32ops_fft_normalised": round(gu32ops(n, 4 * m, ms), 1),
                              "truncated_instances_per_s": round(n / ms_t * 1e3), "truncated_ms": round(ms_t, 4),
+                             "truncated_gu32ops_fft_normalised": round(gu32ops(n, 2 * m, ms_t), 1),
                              "autotuned_full_instances_per_s": round(n / ms_tuned * 1e3),
                              "autotuned_frac_of_intpipe_peak": round(wp / ms_tuned * 1e3 / peak_wps, 4),
                              "autotuned_tiling": {"instances_per_cta": chosen[0], "row_slices": chosen[1]}}
@@ -680,7 +692,9 @@ def measure_reference_kernels(B, L, stream):
         ms_tr = event_time(stream, lambda: R.ref_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, sp), 3)
         ms_ours_tr = event_time(stream, lambda: check(L, L.bi_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, sp)), 3)
         entry = {"truncated_reference_inst_per_s": round(n / ms_tr * 1e3),
-                 "truncated_ours_inst_per_s": round(n / ms_ours_tr * 1e3)}
+                 "truncated_ours_inst_per_s": round(n / ms_ours_tr * 1e3),
+                 "truncated_reference_gu32ops_fft_normalised": round(gu32ops(n, 2 * m, ms_tr), 1),
+                 "truncated_ours_gu32ops_fft_normalised": round(gu32ops(n, 2 * m, ms_ours_tr), 1)}
         if 2 * m in refgpu.MUL_SIZES_U64:
             pa = torch.zeros((n, 2 * m), dtype=torch.int64, device="cuda")
             pb = torch.zeros_like(pa)
@@ -691,6 +705,8 @@ def measure_reference_kernels(B, L, stream):
             ms_ours_f = event_time(stream, lambda: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), rf.data_ptr(), m, n, sp)), 3)
             entry["full_reference_inst_per_s"] = round(n / ms_f * 1e3)
             entry["full_ours_inst_per_s"] = round(n / ms_ours_f * 1e3)
+            entry["full_reference_gu32ops_fft_normalised"] = round(gu32ops(n, 4 * m, ms_f), 1)
+            entry["full_ours_gu32ops_fft_normalised"] = round(gu32ops(n, 4 * m, ms_ours_f), 1)
             del pa, pb, rf
         else:
             entry["full_reference"] = "unavailable: convMul5 at 2m=%d limbs needs >48 KiB static shared memory" % (2 * m)

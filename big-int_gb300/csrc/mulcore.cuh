@@ -54,15 +54,30 @@ __device__ __forceinline__ void mul_cta(const MulGeom& g, uint64_t* smem, uint32
 
     // ---- stage operands: a_s[x], b_s[x + C] (zero padded), per instance
     {
-        const uint32_t total = g.ipc * Lp;
-        for (uint32_t idx = tid; idx < total; idx += blockDim.x) {
-            const uint32_t li = lpdiv.div(idx);
-            const uint32_t x = idx - li * Lp;
-            uint64_t va = 0, vb = 0;
-            if (x < g.L) load(li, x, va, vb);
-            uint64_t* base = smem + (size_t)li * g.IS;
-            base[skew<C>(x)] = va;
-            base[g.SA + skew<C>(x + C)] = vb;
+        // U limbs a thread in flight: all U loads issue before the first
+        // shared-memory store waits on one
+        constexpr int U = 4;
+        const uint32_t total = g.ipc * Lp, step = blockDim.x;
+        for (uint32_t idx0 = tid; idx0 < total; idx0 += U * step) {
+            uint64_t va[U], vb[U];
+            uint32_t li[U], x[U];
+#pragma unroll
+            for (int k = 0; k < U; k++) {
+                const uint32_t idx = idx0 + k * step;
+                li[k] = lpdiv.div(idx);
+                x[k] = idx - li[k] * Lp;
+                va[k] = 0;
+                vb[k] = 0;
+                if (idx < total && x[k] < g.L) load(li[k], x[k], va[k], vb[k]);
+            }
+#pragma unroll
+            for (int k = 0; k < U; k++) {
+                if (idx0 + k * step < total) {
+                    uint64_t* base = smem + (size_t)li[k] * g.IS;
+                    base[skew<C>(x[k])] = va[k];
+                    base[g.SA + skew<C>(x[k] + C)] = vb[k];
+                }
+            }
         }
         // zero pads of b_s: logical [0, C) and [Lp + C, Lp + 2C)
         for (uint32_t idx = tid; idx < g.ipc * 2 * C; idx += blockDim.x) {

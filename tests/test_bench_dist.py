@@ -65,3 +65,13 @@ def test_reference_arm_prints_from_rank_zero_only():
                         "--warmup", "0"], env=env, capture_output=True, text=True, timeout=300)
     assert r.returncode == 0
     assert r.stdout.strip() == ""
+
+
+def test_gu32ops_follows_the_reference_formula():
+    # cuda/main.cu:393-400: num_instances * 300 * M * log2(M) u32 ops over the elapsed microseconds * 1000
+    sys.path.insert(0, REPO)
+    import bench
+
+    n, words, ms = 4096, 128, 0.5
+    assert abs(bench.gu32ops(n, words, ms) - n * 300 * words * 7 / (ms * 1000 * 1000)) < 1e-9
+    assert bench.gu32ops(1, 2, 1e-6) == 300 * 2 * 1   # log2(2) = 1
