@@ -92,6 +92,9 @@ __device__ __forceinline__ uint8_t div_thread(uint32_t MU, uint32_t MV, LoadU lo
     const uint64_t vr = recip_limb(d1);
     int tn = (int)MU - MX - 1;   // shifted-dividend limb that enters the window next
     for (int j = (int)MU - K; j >= 0; j--) {
+        // the raw limb this step's slide needs, loaded first so that its
+        // latency overlaps the step's arithmetic
+        const uint64_t lower = j > 0 ? raw(tn - 1) : 0;
         const uint64_t u2 = R[MX], u1 = R[MX - 1], u0 = R[MX - 2];
         uint64_t qh, rh;
         bool rh_over = false;
@@ -139,8 +142,7 @@ __device__ __forceinline__ uint8_t div_thread(uint32_t MU, uint32_t MV, LoadU lo
         if (j > 0) {                           // slide the window down one limb
 #pragma unroll
             for (int k = MX; k > 0; k--) R[k] = R[k - 1];
-            const uint64_t lower = raw(tn - 1);    // below = raw(tn)
-            R[0] = (below << s) | ((lower >> 1) >> rs);
+            R[0] = (below << s) | ((lower >> 1) >> rs);   // below = raw(tn)
             below = lower;
             tn--;
         }
