@@ -301,11 +301,11 @@ def run_reference(args) -> None:
 
 def div_method(mv: int, n: int, sms: int) -> str:
     """The method bi_div_u64 picks for n divisions by mv-limb divisors
-    (div_use_long in divsmall.cuh): long division on one thread or one lane
-    group (8, 16 or 32 lanes) per instance, or the shifted inverse on one CTA
-    per instance."""
+    (div_small_on_groups and div_use_long in divsmall.cuh): long division on
+    one thread or one lane group (8, 16 or 32 lanes) per instance, or the
+    shifted inverse on one CTA per instance."""
     if mv <= 16:
-        return "long_thread"
+        return "long_group" if mv > 8 and n <= 48 * sms else "long_thread"
     if mv <= 32:
         return "long_group"
     if mv <= 1024 and n > (5 if mv <= 64 else 3 if mv <= 256 else 6) * sms:

@@ -98,10 +98,21 @@ div_thread_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restric
     }
 }
 
+// Several instances a warp: long division on G-lane groups (divsmall.cuh).
+template <typename T, int VPL, int G>
+__global__ void __launch_bounds__(DIV_WARP_CTA)
+div_group_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
+                 uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv);
+
 template <typename T>
 static void launch_div_thread(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
                               uint64_t n, cudaStream_t s) {
     const uint32_t MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    if (div_small_on_groups(MV, n, num_sms())) {   // few instances: four 8-lane groups a warp
+        const uint64_t warps = (n + 3) / 4, blocks = (warps + DIV_WARP_CTA / 32 - 1) / (DIV_WARP_CTA / 32);
+        div_group_kernel<T, 2, 8><<<(unsigned)blocks, DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+        return;
+    }
     const uint64_t blocks = (n + DIV_THREAD_CTA - 1) / DIV_THREAD_CTA;
     const unsigned grid = (unsigned)(blocks < (1u << 20) ? blocks : (1u << 20));
     if (MV <= 2) div_thread_kernel<T, 2><<<grid, DIV_THREAD_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
@@ -131,7 +142,6 @@ div_warp_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict_
     }
 }
 
-// Several instances a warp: long division on G-lane groups (divsmall.cuh).
 template <typename T, int VPL, int G>
 __global__ void __launch_bounds__(DIV_WARP_CTA)
 div_group_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,

@@ -41,6 +41,18 @@ __host__ __device__ inline bool div_use_long(uint32_t MV, uint64_t n, int sms) {
     return n > per_sm * (uint64_t)sms;
 }
 
+// Divisors of 9..16 limbs in a batch of at most DIV_SMALL_GROUP_PER_SM
+// instances an SM run on 8-lane groups (div_group<2, 8>, four instances a
+// warp) instead of one thread each: so few instances leave the GPU short of
+// warps, and one thread's quotient limbs are long.  Measured on GB300 (32/16
+// limbs): 4096 divisions 16.7 us on threads, 11.1 on groups; 16384 of them
+// 19.1 us on threads, 26.1 on groups (a group does about three times a
+// thread's work per instance).
+constexpr int DIV_SMALL_GROUP_PER_SM = 48;
+__host__ __device__ inline bool div_small_on_groups(uint32_t MV, uint64_t n, int sms) {
+    return MV > 8 && MV <= (uint32_t)DIV_THREAD_MAX_MV && n <= (uint64_t)DIV_SMALL_GROUP_PER_SM * (uint64_t)sms;
+}
+
 // One instance: u (MU 64-bit limbs through load_u), v (MV <= MX limbs through
 // load_v); writes MU quotient limbs and MV remainder limbs.  Returns the
 // status: 0, or 1 when v == 0 (then q = r = 0).

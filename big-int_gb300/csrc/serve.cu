@@ -47,6 +47,10 @@ constexpr uint64_t SERVE_LOST = 0xFF;            // status of a request whose sl
 // on the whole CTA (shifted inverse): measured on the serving workload, 64
 // (the single-division crossover) gave p90 40-45 us against 36-38 here
 constexpr uint32_t SERVE_DIV_WARP_MAX_MV = 128;
+// divisors up to this many limbs divide on thread 0: one division alone takes
+// 3.9 us on a thread and 4.3 on a warp at 8/4 limbs, 5.9 and 5.3 at 16/8,
+// 13.7 and 7.9 at 32/16 (GB300)
+constexpr uint32_t SERVE_DIV_THREAD_MAX_MV = 8;
 
 struct alignas(64) ServeSlot {   // one request in the ring (mapped host memory)
     bi_desc d;                   // written first
@@ -245,11 +249,10 @@ __global__ void __launch_bounds__(SERVE_CTA, 2) serve_kernel(const ServeArgs A) 
                 auto st_r = [&](uint32_t i, uint64_t x) { r2[i] = x; };
                 // long division on one thread or one warp where it finishes
                 // sooner than the CTA's shifted inverse (divsmall.cuh)
-                if (d.mb <= (uint32_t)DIV_THREAD_MAX_MV) {
+                if (d.mb <= SERVE_DIV_THREAD_MAX_MV) {
                     if (threadIdx.x == 0) {
                         const uint8_t st = d.mb <= 4 ? div_thread<4>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
-                                                     : d.mb <= 8 ? div_thread<8>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
-                                                                 : div_thread<16>(d.m, d.mb, ld_u, ld_v, st_q, st_r);
+                                                     : div_thread<8>(d.m, d.mb, ld_u, ld_v, st_q, st_r);
                         s_flag = st;
                     }
                 } else if (d.mb <= SERVE_DIV_WARP_MAX_MV) {

@@ -245,3 +245,21 @@ def test_full_size_division_identity(bigint, mv, n):
     assert torch.equal(diff, rpad)
     _, lt = B.sub(r, v)
     assert (lt == 1).all()
+
+
+@pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
+@pytest.mark.parametrize("mv,n", [(9, 40), (12, 3000), (16, 7000), (16, 9000), (12, 20000)])
+def test_small_divisors_on_groups_and_threads(bigint, oracle, dtype, mv, n):
+    """Divisors of 9..16 64-bit limbs: few instances run on 8-lane groups
+    (div_small_on_groups), many on one thread each; both give the oracle's
+    q and r, with add-backs forced on some rows (u = v * B^k - 1 style rows)."""
+    w = 2 if dtype == np.uint32 else 1
+    mu = 2 * mv * w
+    u = uniform_limbs(301 + mv + n, n, mu, dtype)
+    v = uniform_limbs(302 + mv + n, n, mv * w, dtype)
+    v[:, -1] |= 1
+    top = np.iinfo(dtype).max
+    for i in range(0, n, 7):                       # v = B^k - 1 shaped divisors, u all ones
+        v[i, :] = top
+        u[i, :] = top
+    _run(bigint, oracle, u, v, "auto")
