@@ -169,7 +169,8 @@ div_group_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict
 // divisor size that ran fastest on GB300 (2m/m divisions, thousands of
 // instances): 8-lane groups of 4 and 8 limbs a lane up to 32 and 64 limbs,
 // 16-lane groups of 8 up to 128, a whole warp of 8 up to 256, 16-lane groups
-// of 32 up to 512, a warp of 32 up to 1024.
+// of 32 up to 512, a warp of 32 up to 1024; with few instances
+// (div_small_on_warps) one warp each up to 128 limbs.
 template <typename T>
 static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
                             uint64_t n, cudaStream_t s) {
@@ -180,6 +181,12 @@ static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status,
         const uint64_t blocks = (warps + WPC - 1) / WPC;
         return (unsigned)(blocks < (1u << 20) ? blocks : (1u << 20));
     };
+    if (div_small_on_warps(MV, n, num_sms())) {   // few instances: one warp each
+        if (MV <= 32) div_warp_kernel<T, 1><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+        else if (MV <= 64) div_warp_kernel<T, 2><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+        else div_warp_kernel<T, 4><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+        return;
+    }
     if (MV <= 32) div_group_kernel<T, 4, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 64) div_group_kernel<T, 8, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 128) div_group_kernel<T, 8, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);

@@ -31,14 +31,27 @@ constexpr int DIV_WARP_CTA = 128;       // threads per CTA of the one-warp-per-i
 // another (0.4 to 1.5 us a limb), so with few instances one CTA per instance
 // finishes sooner; past a few instances per SM the groups' throughput wins.
 // Measured crossovers (dividend 2 MV limbs, GB300, the shapes div.cu
-// launches): long division always up to 32 limbs; above that once n exceeds
-// 5, 3, 3, 6 and 6 instances per SM for divisors up to 64, 128, 256, 512 and
-// 1024 limbs.
+// launches): long division always up to 64 limbs (with few instances on one
+// warp each: 152 divisions of 128/64 limbs take 30 us, the shifted inverse
+// 40); above that once n exceeds 2, 4, 5 and 4 instances per SM for divisors
+// up to 128, 256, 512 and 1024 limbs.
 __host__ __device__ inline bool div_use_long(uint32_t MV, uint64_t n, int sms) {
-    if (MV <= 32) return true;
+    if (MV <= 64) return true;
     if (MV > (uint32_t)DIV_WARP_MAX_MV) return false;
-    const uint64_t per_sm = MV <= 64 ? 5 : MV <= 256 ? 3 : 6;
+    const uint64_t per_sm = MV <= 128 ? 2 : MV <= 256 ? 4 : MV <= 512 ? 5 : 4;
     return n > per_sm * (uint64_t)sms;
+}
+
+// Divisors of 17..128 limbs in a batch of at most DIV_SMALL_WARP_PER_SM
+// instances an SM divide on one warp each (div_warp with 1, 2 or 4 limbs a
+// lane) instead of sharing warps as lane groups: a warp's quotient limbs are
+// shorter, and with so few instances the GPU has warps to spare.  Measured
+// on GB300 (2m/m limbs; warps vs groups): 64/32, 152 divisions 15.3 vs 19.9
+// us, 3040 of them 27.3 vs 22.6; 128/64, 152: 28.1 vs 44.0, 1520: 39.2 vs
+// 44.2, 3040: 58.3 vs 53.8; 256/128, 760: 70.9 vs 80.3, 3040: 133.9 vs 128.2.
+constexpr int DIV_SMALL_WARP_PER_SM = 10;
+__host__ __device__ inline bool div_small_on_warps(uint32_t MV, uint64_t n, int sms) {
+    return MV > (uint32_t)DIV_THREAD_MAX_MV && MV <= 128 && n <= (uint64_t)DIV_SMALL_WARP_PER_SM * (uint64_t)sms;
 }
 
 // Divisors of 9..16 limbs in a batch of at most DIV_SMALL_GROUP_PER_SM

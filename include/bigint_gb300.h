@@ -137,6 +137,7 @@ bi_status bi_mul_set_tuning_u32(uint32_t m, int full, int ipc, int slices);
 /* 0 = ok, 1 = divisor zero (q_i and r_i are set to 0), 2 = internal      */
 /* correction bound exceeded (never observed).  The reference divides by   */
 /* zero (div.c:165-181); this entry reports it per instance instead.       */
+/* q and r must not overlap u, v or each other.                            */
 /* mu <= bi_max_limbs_div_* ().                                            */
 /* ---------------------------------------------------------------------- */
 uint32_t bi_max_limbs_div_u64(void);

@@ -263,3 +263,17 @@ def test_small_divisors_on_groups_and_threads(bigint, oracle, dtype, mv, n):
         v[i, :] = top
         u[i, :] = top
     _run(bigint, oracle, u, v, "auto")
+
+
+@pytest.mark.parametrize("method", ["auto", "long"])
+@pytest.mark.parametrize("mv,n", [(20, 100), (32, 2000), (50, 300), (64, 2000), (100, 40), (128, 2000)])
+def test_small_batches_on_warps_large_on_groups(bigint, oracle, mv, n, method):
+    """Divisors of 17..128 limbs: up to 10 instances an SM divide on one warp
+    each (div_small_on_warps), more on shared lane groups; the same (q, r)."""
+    u = uniform_limbs(311 + mv + n, n, 2 * mv)
+    v = uniform_limbs(312 + mv + n, n, mv)
+    v[:, -1] |= np.uint64(1)
+    for i in range(0, n, 5):                       # all-ones rows: the estimate's q-hat = B - 1 branch
+        v[i, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        u[i, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    _run(bigint, oracle, u, v, method)
