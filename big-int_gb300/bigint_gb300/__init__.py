@@ -286,9 +286,11 @@ def div(u, v, q=None, r=None, status=None, stream=None, method="auto"):
 
 
 def mul_autotune(a, b, r=None, full: bool = True, reps: int = 3, stream=None):
-    """Time the CTA multiply's tilings on (a, b), keep the fastest for this
-    (limb width, full, m); returns (instances per CTA, slices), (0, 0) where
-    the warp kernel runs.  r receives the product as mulfull/mul write it."""
+    """Time the CTA multiply's tilings on (a, b) -- and the 32-bit-word warp
+    kernel for full products of at most 32 64-bit limbs -- and keep the
+    fastest for this (limb width, full, m); returns (instances per CTA,
+    slices), or (0, 0) when the warp kernel was fastest.  r receives the
+    product as mulfull/mul write it."""
     import torch
 
     _dev2d(a, "a"), _dev2d(b, "b")

@@ -396,7 +396,10 @@ template <typename T, bool FULL>
 static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
-    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, st);
+    if (FULL && L <= MUL_WARP_MAX_L) {   // the warp kernel unless a tiling of the CTA kernel was tuned for m
+        MulTune t;
+        if (!mul_tuning_lookup((int)sizeof(T), FULL, L, &t) || t.ipc == 0) return mul_warp<T>(a, b, r, m, n, st);
+    }
     return mul_launch_geom<T, FULL>(a, b, r, m, n, mul_geom_for<T, FULL>(L, n), st);
 }
 
@@ -439,32 +442,42 @@ static bi_status mul_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n,
 
 // Time every tiling that fits (ipc in 1, 2, 4, ..., S in 1, 2, 4) on the
 // caller's operands, median of `reps` runs each, and record the fastest.
+// For full products of at most MUL_WARP_MAX_L 64-bit limbs the warp kernel
+// (32-bit words: mad.lo/madc.hi column sums) is a candidate too, recorded as
+// ipc = 0, beside the CTA kernel's tilings (64-bit limbs: row_mac8) -- the
+// arithmetic's word width is part of what is tuned.
 template <typename T, bool FULL>
 static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t n, int reps, int* chosen,
                               cudaStream_t st) {
     if (chosen) chosen[0] = chosen[1] = 0;
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
-    if (FULL && L <= MUL_WARP_MAX_L) return mul_warp<T>(a, b, r, m, n, st);   // the warp kernel: nothing to tile
+    const bool warp_ok = FULL && L <= MUL_WARP_MAX_L;
     std::vector<std::pair<uint32_t, uint32_t>> cands;
+    if (warp_ok) cands.push_back({0, 0});
     for (uint32_t ipc = 1; ipc <= 64; ipc *= 2)
         for (uint32_t S = 1; S <= 4; S *= 2) {
             MulGeom g;
             if (mul_geom_tiled(L, FULL, ipc, S, &g) && (uint64_t)ipc <= n) cands.push_back({ipc, S});
         }
     if (cands.empty()) return set_error(BI_EUNSUPPORTED, "mul autotune: no tiling fits m=%u", m);
+    // one run of a candidate: the warp kernel (ipc = 0) or a CTA tiling
+    auto run = [&](uint32_t ipc, uint32_t S) -> bi_status {
+        if (ipc == 0) return mul_warp<T>(a, b, r, m, n, st);
+        MulGeom g;
+        mul_geom_tiled(L, FULL, ipc, S, &g);
+        return mul_launch_geom<T, FULL>(a, b, r, m, n, g, st);
+    };
     cudaEvent_t e0, e1;
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return set_error(BI_ECUDA, "mul autotune: %s", cudaGetErrorString(cudaGetLastError()));
     float best = 1e30f;
-    MulTune pick = {0, 0};
+    MulTune pick = cands[0].first == 0 ? MulTune{0, 0} : MulTune{cands[0].first, cands[0].second};
     bi_status st_out = BI_OK;
     for (const auto& c : cands) {
-        MulGeom g;
-        mul_geom_tiled(L, FULL, c.first, c.second, &g);
         std::vector<float> ts;
         for (int k = 0; k <= reps && st_out == BI_OK; k++) {   // the first run warms up
             cudaEventRecord(e0, st);
-            st_out = mul_launch_geom<T, FULL>(a, b, r, m, n, g, st);
+            st_out = run(c.first, c.second);
             cudaEventRecord(e1, st);
             if (cudaEventSynchronize(e1) != cudaSuccess) st_out = set_error(BI_ECUDA, "mul autotune: %s",
                                                                             cudaGetErrorString(cudaGetLastError()));
@@ -490,9 +503,7 @@ static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t
         g_tune[std::make_tuple(dev, (int)sizeof(T), FULL ? 1 : 0, L)] = pick;
     }
     // leave r as one plain call with the chosen tiling writes it
-    MulGeom g;
-    mul_geom_tiled(L, FULL, pick.ipc, pick.S, &g);
-    BI_RETURN_IF((mul_launch_geom<T, FULL>(a, b, r, m, n, g, st)));
+    BI_RETURN_IF(run(pick.ipc, pick.S));
     if (chosen) {
         chosen[0] = (int)pick.ipc;
         chosen[1] = (int)pick.S;

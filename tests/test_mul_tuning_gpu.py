@@ -12,7 +12,8 @@ pytestmark = pytest.mark.gpu
 @pytest.fixture(autouse=True)
 def _reset(bigint):
     yield
-    for m, dt in ((64, np.uint64), (100, np.uint64), (256, np.uint64), (200, np.uint32), (16, np.uint64)):
+    for m, dt in ((64, np.uint64), (100, np.uint64), (256, np.uint64), (200, np.uint32), (16, np.uint64),
+                  (2, np.uint64), (4, np.uint64), (32, np.uint64), (40, np.uint32)):
         for full in (False, True):
             bigint.mul_set_tuning(m, dt, full, 0)
 
@@ -56,12 +57,38 @@ def test_autotune_result_and_later_calls(bigint, oracle, m, dtype):
         assert (B.to_host(r, dtype) == ref).all()
 
 
-def test_autotune_warp_sizes_have_nothing_to_tile(bigint, oracle):
+@pytest.mark.parametrize("m,dtype", [(16, np.uint64), (2, np.uint64), (32, np.uint64), (40, np.uint32)])
+def test_autotune_weighs_the_warp_kernel_at_small_sizes(bigint, oracle, m, dtype):
+    """Full products of at most 32 64-bit limbs: the autotuner times the warp
+    kernel (32-bit words, reported as (0, 0)) beside the CTA tilings (64-bit
+    limbs); r and every later call are exact whichever wins."""
     B = bigint
-    a = uniform_limbs(901, 50, 16)
-    b = uniform_limbs(902, 50, 16)
     import torch
+    n = 500
+    a = uniform_limbs(901 + m, n, m, dtype)
+    b = uniform_limbs(902 + m, n, m, dtype)
+    a[0] = np.iinfo(dtype).max
+    b[0] = np.iinfo(dtype).max
     da, db = B.to_device(a), B.to_device(b)
-    r = torch.zeros((50, 32), dtype=torch.int64, device="cuda")
-    assert B.mul_autotune(da, db, r, full=True, reps=1) == (0, 0)
-    assert (B.to_host(r, np.uint64) == oracle.mulfull(a, b)).all()
+    r = torch.zeros((n, 2 * m), dtype=torch.int64 if dtype == np.uint64 else torch.int32, device="cuda")
+    ipc, slices = B.mul_autotune(da, db, r, full=True, reps=2)
+    assert (ipc, slices) == (0, 0) or (ipc >= 1 and slices in (1, 2, 4))
+    assert (B.to_host(r, dtype) == oracle.mulfull(a, b)).all()
+    assert (B.to_host(B.mulfull(da, db), dtype) == oracle.mulfull(a, b)).all()
+    B.mul_set_tuning(m, dtype, True, 0)
+
+
+@pytest.mark.parametrize("m", [4, 16, 32])
+def test_cta_tiling_by_hand_at_warp_sizes(bigint, oracle, m):
+    """A tiling set by hand for a small full product moves it from the warp
+    kernel to the CTA kernel; clearing it moves it back; both exact."""
+    B = bigint
+    n = 77
+    a = uniform_limbs(911 + m, n, m)
+    b = uniform_limbs(912 + m, n, m)
+    da, db = B.to_device(a), B.to_device(b)
+    ref = oracle.mulfull(a, b)
+    B.mul_set_tuning(m, np.uint64, True, 2, 1)
+    assert (B.to_host(B.mulfull(da, db), np.uint64) == ref).all()
+    B.mul_set_tuning(m, np.uint64, True, 0)
+    assert (B.to_host(B.mulfull(da, db), np.uint64) == ref).all()
