@@ -113,6 +113,8 @@ SIGNATURES: dict[str, list] = {
     "bi_plan_execute": [_P, _P, _P, _P, _P],
     "bi_plan_autotune": [_P, _P, _P, _P, _I, _P],
     "bi_plan_set_tuning": [_P, _I, _I, _I],
+    "bi_plan_set_mul_word_bits": [_P, _I],
+    "bi_plan_get_tuning": [_P, _P],
     "bi_plan_stats": [_P, _P],
     "bi_plan_destroy": [_P],
     "bi_batch_noalloc_max_descs": [],
@@ -461,10 +463,21 @@ class Plan:
         _check(lib().bi_plan_autotune(self._h, arena_in.data_ptr(), arena_out.data_ptr(),
                                       flags.data_ptr() if flags is not None else None, reps,
                                       ctypes.cast(chosen, ctypes.c_void_p)))
-        return {"addsub_rows": chosen[0], "addsub_limbs_per_lane_row": chosen[1], "mul_ipc_divisor": chosen[2]}
+        return self.tuning()
 
     def set_tuning(self, rows: int, vec: int, ipc_div: int):
         _check(lib().bi_plan_set_tuning(self._h, rows, vec, ipc_div))
+
+    def set_mul_word_bits(self, bits: int):
+        """Word width of the arithmetic for full products of at most 32
+        limbs: 32 (the warp kernel) or 64 (the CTA kernel)."""
+        _check(lib().bi_plan_set_mul_word_bits(self._h, bits))
+
+    def tuning(self) -> dict:
+        t = (ctypes.c_int * 4)()
+        _check(lib().bi_plan_get_tuning(self._h, ctypes.cast(t, ctypes.c_void_p)))
+        return {"addsub_rows": t[0], "addsub_limbs_per_lane_row": t[1], "mul_ipc_divisor": t[2],
+                "mul_small_word_bits": t[3]}
 
     def stats(self) -> dict:
         st = (ctypes.c_uint64 * 6)()

@@ -34,6 +34,7 @@
 #include "divcore.cuh"
 #include "divsmall.cuh"
 #include "mulcore.cuh"
+#include "mulwarp.cuh"
 #include "warpops.cuh"
 
 namespace bi {
@@ -48,10 +49,22 @@ struct MulItem {
 };
 
 struct BatchTune {
-    int addsub_rows;   // rows of 32 lanes loaded per step (limbs per lane = rows * VEC)
-    int addsub_vec;    // limbs per lane per row: 2 (16-byte accesses) or 1
-    int mul_ipc_div;   // divide the default instances-per-CTA by this
+    int addsub_rows;      // rows of 32 lanes loaded per step (limbs per lane = rows * VEC)
+    int addsub_vec;       // limbs per lane per row: 2 (16-byte accesses) or 1
+    int mul_ipc_div;      // divide the default instances-per-CTA by this
+    int mul_small_bits;   // word width of the full products of at most 32 limbs: 32 (the
+                          // warp kernel, mulwarp.cuh) or 64 (the CTA kernel, mulcore.cuh)
 };
+
+// Full products of at most MULW_MAX_M 64-bit limbs form MULW_CLASSES classes
+// for the warp kernel: class c takes m <= 2 << c on groups of G = 2 << c lanes.
+constexpr int MULW_CLASSES = 5;
+constexpr uint32_t MULW_MAX_M = 32;
+inline int mulw_class(uint32_t m) {
+    int c = 0;
+    while ((2u << c) < m) c++;
+    return c;
+}
 
 template <int VEC, int R>
 __global__ void __launch_bounds__(256)
@@ -127,6 +140,42 @@ batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
     }
 }
 
+// Small full products (class of G, at most G 64-bit limbs) on the warp
+// kernel's 32-bit word arithmetic (mulwarp.cuh): G-lane groups, 32 / G
+// instances a warp; lane 0 takes that many list entries at a time.
+template <int G>
+__global__ void __launch_bounds__(MUL_WARP_CTA)
+batch_mulwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                     uint32_t* counter, const uint64_t* in, uint64_t* out) {
+    constexpr uint32_t ipw = 32 / G;
+    extern __shared__ __align__(16) uint32_t smw[];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t lg = lane / G, t = lane - lg * G;
+    uint32_t* sw = smw + ((size_t)warp * ipw + lg) * mul_warp_group_words<G>();
+    for (;;) {
+        uint32_t idx0 = 0;
+        if (lane == 0) idx0 = atomicAdd(counter, ipw);
+        idx0 = __shfl_sync(0xffffffffu, idx0, 0);
+        if (idx0 >= count) break;
+        const uint32_t idx = idx0 + lg;
+        bi_desc d = {};                       // a group past the list: m = 0, loads zeros, stores nothing
+        if (idx < count) d = descs[list[idx]];
+        const uint64_t* pa = in + d.a;
+        const uint64_t* pb = in + d.b;
+        uint64_t* pr = out + d.r;
+        const uint32_t words = 2 * d.m;
+        mul_warp_group<G>(
+            sw, t, lg * G,
+            [&](uint32_t x, uint32_t& wa, uint32_t& wb) {
+                wa = x < words ? (uint32_t)(pa[x >> 1] >> (32 * (x & 1))) : 0u;
+                wb = x < words ? (uint32_t)(pb[x >> 1] >> (32 * (x & 1))) : 0u;
+            },
+            [&](uint32_t c, uint64_t v) {
+                if (c < 2 * d.m) pr[c] = v;
+            });
+    }
+}
+
 // division classes by divisor limbs: long division on threads (divisors up
 // to 4, 8, 16 limbs), on warps (up to 32, 64, ..., 1024 limbs), the shifted
 // inverse on 512-thread CTAs above
@@ -134,7 +183,9 @@ constexpr int DIV_THREAD_CLASSES = 3, DIV_WARP_CLASSES = 6;
 constexpr int DIV_CTA_CLASS = DIV_THREAD_CLASSES + DIV_WARP_CLASSES;
 constexpr int DIV_CLASSES = DIV_CTA_CLASS + 1;
 constexpr int DIV_CTA_THREADS = 512;
-constexpr int PLAN_KERNELS = 2 + DIV_CLASSES;   // add/sub, multiply, one per division class
+// add/sub, multiply, one per division class, one per warp-multiply class
+constexpr int PLAN_KERNELS = 2 + DIV_CLASSES + MULW_CLASSES;
+constexpr int PLAN_MULW0 = 2 + DIV_CLASSES;      // index of the first warp-multiply kernel
 
 static inline int div_class(uint32_t mv) {
     if (mv <= 4) return 0;
@@ -275,18 +326,21 @@ struct bi_plan {
     uint32_t* d_addsub = nullptr;
     uint32_t* d_mul = nullptr;
     uint32_t* d_div = nullptr;          // division list: class 0, then 1, then 2
-    MulItem* d_items = nullptr;
-    uint32_t* d_counters = nullptr;     // add/sub, multiply, one per division class
-    uint32_t n_addsub = 0, n_mul = 0, n_items = 0, n_div = 0;
+    MulItem* d_items = nullptr;         // every multiply, on the CTA kernel
+    MulItem* d_items_large = nullptr;   // the multiplies the warp classes do not take
+    uint32_t* d_mulw = nullptr;         // small full products: warp class 0, then 1, ...
+    uint32_t* d_counters = nullptr;     // one per kernel (PLAN_KERNELS)
+    uint32_t n_addsub = 0, n_mul = 0, n_items = 0, n_div = 0, n_items_large = 0, n_mulw_total = 0;
+    uint32_t mulw_off[MULW_CLASSES] = {}, n_mulw[MULW_CLASSES] = {};
     uint32_t div_off[DIV_CLASSES] = {}, n_divc[DIV_CLASSES] = {};
     uint32_t max_mul_Lp_full = 0, max_mul_Lp_trunc = 0;
     size_t mul_smem = 0, div_smem = 0, divc_smem[DIV_CLASSES] = {};
-    BatchTune tune = {4, 2, 1};
+    BatchTune tune = {4, 2, 1, 32};
     cudaGraphExec_t exec = nullptr;
     const void* g_in = nullptr;
     void* g_out = nullptr;
     void* g_flags = nullptr;
-    BatchTune g_tune = {0, 0, 0};
+    BatchTune g_tune = {0, 0, 0, 0};
     cudaStream_t cap = nullptr;
     cudaStream_t side[PLAN_KERNELS] = {};
     cudaEvent_t ev_fork = nullptr, ev_join[PLAN_KERNELS] = {};
@@ -368,7 +422,7 @@ static bi_status grid_for(const void* k, int threads, size_t smem, uint64_t work
     int occ = 1;
     if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, smem) != cudaSuccess)
-        return set_error(BI_ECUDA, "batch div kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
+        return set_error(BI_ECUDA, "batch kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
     *grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(work_ctas, (uint64_t)sms * (occ < 1 ? 1 : occ)));
     return BI_OK;
 }
@@ -390,10 +444,28 @@ static const void* div_class_kernel(int c, int* threads) {
     }
 }
 
+// Whether tuning t sends the plan's small full products to the warp kernel.
+static bool plan_small_on_warps(const bi_plan* p, const BatchTune& t) {
+    return t.mul_small_bits == 32 && p->n_mulw_total > 0;
+}
+
+// The warp-multiply kernel of class c (host-side function pointer).
+static const void* mulw_class_kernel(int c) {
+    switch (c) {
+    case 0: return (const void*)batch_mulwarp_kernel<2>;
+    case 1: return (const void*)batch_mulwarp_kernel<4>;
+    case 2: return (const void*)batch_mulwarp_kernel<8>;
+    case 3: return (const void*)batch_mulwarp_kernel<16>;
+    default: return (const void*)batch_mulwarp_kernel<32>;
+    }
+}
+
 // Grid sizes and shared memory of the kernels for tuning t; sets the
 // kernels' shared-memory limits (done outside any stream capture).
 static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
     const int sms = num_sms();
+    const bool small_warp = plan_small_on_warps(p, t);
+    const uint32_t n_items = small_warp ? p->n_items_large : p->n_items;
     L->grid[0] = (unsigned)std::min<uint64_t>((p->n_addsub + 7) / 8, (uint64_t)sms * 8);
     L->smem[0] = 0;
     L->smem[1] = mul_smem_for(p, t.mul_ipc_div);
@@ -401,12 +473,26 @@ static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
         L->smem[2 + c] = p->divc_smem[c];
         L->grid[2 + c] = 0;
     }
+    for (int c = 0; c < MULW_CLASSES; c++) {
+        L->smem[PLAN_MULW0 + c] = 0;
+        L->grid[PLAN_MULW0 + c] = 0;
+    }
     int occ = 1;
-    if (p->n_items) {
+    L->grid[1] = 0;
+    if (n_items) {
         if (cudaFuncSetAttribute(batch_mul_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L->smem[1]) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_mul_kernel, BATCH_CTA, L->smem[1]) != cudaSuccess)
             return set_error(BI_ECUDA, "batch mul kernel setup: %s", cudaGetErrorString(cudaGetLastError()));
-        L->grid[1] = (unsigned)std::min<uint64_t>(p->n_items, (uint64_t)sms * (occ < 1 ? 1 : occ));
+        L->grid[1] = (unsigned)std::min<uint64_t>(n_items, (uint64_t)sms * (occ < 1 ? 1 : occ));
+    }
+    for (int c = 0; small_warp && c < MULW_CLASSES; c++) {
+        const uint64_t n = p->n_mulw[c];
+        if (!n) continue;
+        const uint32_t G = 2u << c, ipw = 32 / G, warps = MUL_WARP_CTA / 32;
+        const size_t smem = (size_t)warps * ipw * (3 * 2 * G) * sizeof(uint32_t);
+        L->smem[PLAN_MULW0 + c] = smem;
+        BI_RETURN_IF(grid_for(mulw_class_kernel(c), MUL_WARP_CTA, smem, (n + warps * ipw - 1) / (warps * ipw), sms,
+                              &L->grid[PLAN_MULW0 + c]));
     }
     for (int c = 0; c < DIV_CLASSES; c++) {
         const uint64_t n = p->n_divc[c];
@@ -440,10 +526,32 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
             batch_addsub_kernel<1, 4><<<grid, 256, 0, s_add>>>(p->d_descs, p->d_addsub, p->n_addsub, p->d_counters + 0, in, out, flags);
         BI_RETURN_IF(check_launch("batch add/sub kernel"));
     }
-    if (p->n_items && (comps & COMP_MUL)) {
-        batch_mul_kernel<<<L.grid[1], BATCH_CTA, L.smem[1], s_mul>>>(p->d_descs, p->d_mul, p->d_items, p->n_items,
-                                                                     p->d_counters + 1, in, out, t.mul_ipc_div);
-        BI_RETURN_IF(check_launch("batch mul kernel"));
+    if (comps & COMP_MUL) {
+        const bool small_warp = plan_small_on_warps(p, t);
+        const MulItem* items = small_warp ? p->d_items_large : p->d_items;
+        const uint32_t n_items = small_warp ? p->n_items_large : p->n_items;
+        if (n_items) {
+            batch_mul_kernel<<<L.grid[1], BATCH_CTA, L.smem[1], s_mul>>>(p->d_descs, p->d_mul, items, n_items,
+                                                                         p->d_counters + 1, in, out, t.mul_ipc_div);
+            BI_RETURN_IF(check_launch("batch mul kernel"));
+        }
+        for (int c = 0; small_warp && c < MULW_CLASSES; c++) {
+            const uint32_t n = p->n_mulw[c];
+            if (!n) continue;
+            const uint32_t* list = p->d_mulw + p->mulw_off[c];
+            uint32_t* ctr = p->d_counters + PLAN_MULW0 + c;
+            const unsigned grid = L.grid[PLAN_MULW0 + c];
+            const size_t smem = L.smem[PLAN_MULW0 + c];
+            cudaStream_t st = s[PLAN_MULW0 + c];
+            switch (c) {
+            case 0: batch_mulwarp_kernel<2><<<grid, MUL_WARP_CTA, smem, st>>>(p->d_descs, list, n, ctr, in, out); break;
+            case 1: batch_mulwarp_kernel<4><<<grid, MUL_WARP_CTA, smem, st>>>(p->d_descs, list, n, ctr, in, out); break;
+            case 2: batch_mulwarp_kernel<8><<<grid, MUL_WARP_CTA, smem, st>>>(p->d_descs, list, n, ctr, in, out); break;
+            case 3: batch_mulwarp_kernel<16><<<grid, MUL_WARP_CTA, smem, st>>>(p->d_descs, list, n, ctr, in, out); break;
+            default: batch_mulwarp_kernel<32><<<grid, MUL_WARP_CTA, smem, st>>>(p->d_descs, list, n, ctr, in, out);
+            }
+            BI_RETURN_IF(check_launch("batch warp mul kernel"));
+        }
     }
     if (comps & COMP_DIV) {
         // the largest class first: its divisions take longest
@@ -521,6 +629,8 @@ static void plan_free(bi_plan* p) {
     cudaFree(p->d_mul);
     cudaFree(p->d_div);
     cudaFree(p->d_items);
+    cudaFree(p->d_items_large);
+    cudaFree(p->d_mulw);
     cudaFree(p->d_counters);
     for (int k = 0; k < PLAN_KERNELS; k++) {
         if (p->side[k]) cudaStreamDestroy(p->side[k]);
@@ -543,7 +653,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     bi_plan* p = new bi_plan();
     cudaGetDevice(&p->device);
     p->count = count;
-    std::vector<uint32_t> addsub, div;
+    std::vector<uint32_t> addsub, div, mulw[MULW_CLASSES];
     std::vector<std::pair<uint64_t, uint32_t>> mulkeys;   // (bucket key, index)
     for (uint64_t i = 0; i < count; i++) {
         const bi_desc& d = descs[i];
@@ -564,6 +674,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
             if (full) p->max_mul_Lp_full = std::max(p->max_mul_Lp_full, Lp);
             else p->max_mul_Lp_trunc = std::max(p->max_mul_Lp_trunc, Lp);
             mulkeys.push_back({((uint64_t)full << 40) | ((uint64_t)Lp << 8), (uint32_t)i});
+            if (full && d.m <= MULW_MAX_M) mulw[mulw_class(d.m)].push_back((uint32_t)i);
             break;
         }
         case BI_OP_DIV:
@@ -588,7 +699,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
         return x.first > y.first;
     });
     std::vector<uint32_t> mul;
-    std::vector<MulItem> items;
+    std::vector<MulItem> items, items_large;   // all multiplies; those the warp classes do not take
     for (size_t k = 0; k < mulkeys.size();) {
         const uint64_t key = mulkeys[k].first;
         const uint32_t full = (uint32_t)(key >> 40), Lp = (uint32_t)((key >> 8) & 0xffffffffu);
@@ -603,9 +714,20 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
             it.full = full;
             for (size_t j = s; j < s + it.count; j++) mul.push_back(mulkeys[j].second);
             items.push_back(it);
+            if (!(full && Lp <= MULW_MAX_M)) items_large.push_back(it);   // Lp <= 32 iff m <= 32
         }
         k = end;
     }
+    // the warp classes' lists, largest first within a class, one after another
+    std::vector<uint32_t> mulw_all;
+    for (int c = 0; c < MULW_CLASSES; c++) {
+        std::stable_sort(mulw[c].begin(), mulw[c].end(), [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
+        p->mulw_off[c] = (uint32_t)mulw_all.size();
+        p->n_mulw[c] = (uint32_t)mulw[c].size();
+        mulw_all.insert(mulw_all.end(), mulw[c].begin(), mulw[c].end());
+    }
+    p->n_mulw_total = (uint32_t)mulw_all.size();
+    p->n_items_large = (uint32_t)items_large.size();
     p->n_addsub = (uint32_t)addsub.size();
     p->n_mul = (uint32_t)mul.size();
     p->n_items = (uint32_t)items.size();
@@ -629,6 +751,8 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     if (st == BI_OK) st = dev_upload(&p->d_mul, mul, p->cap);
     if (st == BI_OK) st = dev_upload(&p->d_div, div, p->cap);
     if (st == BI_OK) st = dev_upload(&p->d_items, items, p->cap);
+    if (st == BI_OK) st = dev_upload(&p->d_items_large, items_large, p->cap);
+    if (st == BI_OK) st = dev_upload(&p->d_mulw, mulw_all, p->cap);
     if (st == BI_OK) {
         std::vector<uint32_t> zeros(PLAN_KERNELS, 0);
         st = dev_upload(&p->d_counters, zeros, p->cap);
@@ -649,7 +773,27 @@ bi_status bi_plan_set_tuning(bi_plan* p, int addsub_rows, int addsub_vec, int mu
         return set_error(BI_EINVAL, "tuning out of range");
     if (addsub_vec == 1) addsub_rows = 4;
     std::lock_guard<std::mutex> lk(p->mu);
-    p->tune = {addsub_rows, addsub_vec, mul_ipc_div};
+    p->tune.addsub_rows = addsub_rows;
+    p->tune.addsub_vec = addsub_vec;
+    p->tune.mul_ipc_div = mul_ipc_div;
+    return BI_OK;
+}
+
+bi_status bi_plan_set_mul_word_bits(bi_plan* p, int bits) {
+    if (!p) return set_error(BI_EINVAL, "NULL plan");
+    if (bits != 32 && bits != 64) return set_error(BI_EINVAL, "word bits must be 32 or 64");
+    std::lock_guard<std::mutex> lk(p->mu);
+    p->tune.mul_small_bits = bits;
+    return BI_OK;
+}
+
+bi_status bi_plan_get_tuning(bi_plan* p, int* tuning) {
+    if (!p || !tuning) return set_error(BI_EINVAL, "NULL argument");
+    std::lock_guard<std::mutex> lk(p->mu);
+    tuning[0] = p->tune.addsub_rows;
+    tuning[1] = p->tune.addsub_vec;
+    tuning[2] = p->tune.mul_ipc_div;
+    tuning[3] = p->tune.mul_small_bits;
     return BI_OK;
 }
 
@@ -668,7 +812,9 @@ bi_status bi_plan_execute(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t
     return BI_OK;
 }
 
-// Time one component of the plan with tuning t (ms per run, median of reps).
+// Time the plan's components `comp` with tuning t (ms per run, median of
+// reps), their kernels forked onto the plan's streams as the captured graph
+// runs them, so that kernels that share the GPU are timed sharing it.
 static float time_component(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags, const BatchTune& t,
                             int comp, int reps) {
     cudaEvent_t e0, e1;
@@ -680,9 +826,13 @@ static float time_component(bi_plan* p, const uint64_t* in, uint64_t* out, uint8
     for (int r = 0; r < reps + 1; r++) {
         cudaMemsetAsync(p->d_counters, 0, PLAN_KERNELS * sizeof(uint32_t), p->cap);
         cudaEventRecord(e0, p->cap);
-        cudaStream_t ss[PLAN_KERNELS];
-        for (int k = 0; k < PLAN_KERNELS; k++) ss[k] = p->cap;
-        bi_status st = launch_plan_kernels(p, in, out, flags, t, L, ss, comp);
+        cudaEventRecord(p->ev_fork, p->cap);
+        for (int k = 0; k < PLAN_KERNELS; k++) cudaStreamWaitEvent(p->side[k], p->ev_fork, 0);
+        bi_status st = launch_plan_kernels(p, in, out, flags, t, L, p->side, comp);
+        for (int k = 0; k < PLAN_KERNELS; k++) {
+            cudaEventRecord(p->ev_join[k], p->side[k]);
+            cudaStreamWaitEvent(p->cap, p->ev_join[k], 0);
+        }
         cudaEventRecord(e1, p->cap);
         cudaEventSynchronize(e1);
         float ms = 0;
@@ -697,8 +847,12 @@ static float time_component(bi_plan* p, const uint64_t* in, uint64_t* out, uint8
 }
 
 // Pick, on this plan's own data, the add/sub rows per step (limbs per lane)
-// and limb width per lane, and the multiply instances per CTA; results land
-// in `out` exactly as an execute would write them.
+// and limb width per lane, the multiply instances per CTA, and the word
+// width of the small full products' arithmetic (32-bit words on the warp
+// kernel or 64-bit limbs on the CTA kernel), one after another, each
+// candidate timed as a run of the whole plan (its kernels sharing the GPU as
+// in an execute); results land in `out` exactly as an execute would write
+// them.
 bi_status bi_plan_autotune(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t* flags, int reps,
                            int* chosen) {
     if (!p) return set_error(BI_EINVAL, "NULL plan");
@@ -714,7 +868,7 @@ bi_status bi_plan_autotune(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_
             BatchTune t = best;
             t.addsub_rows = c[0];
             t.addsub_vec = c[1];
-            const float ms = time_component(p, in, out, flags, t, COMP_ADDSUB, reps);
+            const float ms = time_component(p, in, out, flags, t, COMP_ALL, reps);
             if (ms < bt) { bt = ms; best.addsub_rows = c[0]; best.addsub_vec = c[1]; }
         }
     }
@@ -724,8 +878,17 @@ bi_status bi_plan_autotune(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_
             BatchTune t = best;
             t.mul_ipc_div = d;
             if (mul_smem_for(p, d) > 227 * 1024) continue;
-            const float ms = time_component(p, in, out, flags, t, COMP_MUL, reps);
+            const float ms = time_component(p, in, out, flags, t, COMP_ALL, reps);
             if (ms < bt) { bt = ms; best.mul_ipc_div = d; }
+        }
+    }
+    if (p->n_mulw_total) {   // the small full products' word width: the warp kernel's 32 or the CTA's 64
+        float bt = 1e30f;
+        for (int bits : {32, 64}) {
+            BatchTune t = best;
+            t.mul_small_bits = bits;
+            const float ms = time_component(p, in, out, flags, t, COMP_ALL, reps);
+            if (ms < bt) { bt = ms; best.mul_small_bits = bits; }
         }
     }
     cudaError_t e = cudaStreamSynchronize(p->cap);

@@ -325,14 +325,25 @@ bi_status bi_plan_create(bi_plan** plan, const bi_desc* descs, uint64_t count);
 /* one plan are serialised; its launches must not overlap on the device.   */
 bi_status bi_plan_execute(bi_plan* plan, const uint64_t* in, uint64_t* out,
                           uint8_t* flags, bi_stream stream);
-/* Time candidate configurations on this plan's data and keep the fastest: */
+/* Time candidate configurations on this plan's data (each as a run of   */
+/* the whole plan, its kernels sharing the GPU) and keep the fastest:      */
 /* add/sub rows per step (2/4/8 x 16 bytes per lane) and limb width per    */
-/* lane (8 or 16 bytes), multiply instances per CTA (default / 2 / 4).     */
-/* chosen (may be NULL) receives {rows, limbs per lane, ipc divisor}.      */
+/* lane (8 or 16 bytes), multiply instances per CTA (default / 2 / 4),    */
+/* and the word width of the arithmetic for full products of at most 32   */
+/* limbs (32-bit words on the warp kernel, 64-bit limbs on the CTA        */
+/* kernel).  chosen (may be NULL) receives {rows, limbs per lane, ipc     */
+/* divisor}; bi_plan_get_tuning returns all four choices.                 */
 bi_status bi_plan_autotune(bi_plan* plan, const uint64_t* in, uint64_t* out,
                            uint8_t* flags, int reps, int* chosen);
 bi_status bi_plan_set_tuning(bi_plan* plan, int addsub_rows, int addsub_vec,
                              int mul_ipc_div);
+/* Full products of at most 32 limbs computed on 32-bit words (bits = 32,   */
+/* the warp kernel; the default) or 64-bit limbs (bits = 64, the CTA       */
+/* kernel with the rest).                                                  */
+bi_status bi_plan_set_mul_word_bits(bi_plan* plan, int bits);
+/* tuning[0..3] = add/sub rows, limbs per lane, multiply ipc divisor,      */
+/* word bits of the small full products.                                   */
+bi_status bi_plan_get_tuning(bi_plan* plan, int* tuning);
 /* stats[0..5] = add/sub instances, multiply instances, multiply items,    */
 /* divisions, multiply and divide shared-memory bytes per CTA.             */
 bi_status bi_plan_stats(const bi_plan* plan, uint64_t* stats);

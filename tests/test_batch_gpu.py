@@ -235,3 +235,64 @@ def test_invalid_descriptors_rejected(bigint):
     empty = B.Plan(np.zeros(0, dtype=B.DESC_DTYPE))
     assert empty.stats()["addsub"] == 0
     empty.close()
+
+
+def _small_mul_batch(B, n=600, seed=91):
+    """Full products of 1..32 limbs (every warp class, odd sizes), with some
+    truncated and larger full products and additions between them."""
+    rng = np.random.default_rng(seed)
+    d = np.zeros(n, dtype=B.DESC_DTYPE)
+    pos = 0
+    out = 0
+    for i in range(n):
+        kind = i % 6
+        m = int(rng.integers(1, 33)) if kind < 4 else int(rng.integers(33, 80))
+        op = B.OP_MULFULL if kind in (0, 1, 2, 4) else (B.OP_MUL if kind == 3 else B.OP_ADD)
+        d[i]["op"], d[i]["m"], d[i]["mb"] = op, m, m
+        d[i]["a"], d[i]["b"] = pos, pos + m
+        pos += 2 * m
+        d[i]["r"] = out
+        out += 2 * m if op == B.OP_MULFULL else m
+    arena = rng.integers(0, 2**64, size=pos, dtype=np.uint64)
+    arena[: 2 * 32] = np.uint64(0xFFFFFFFFFFFFFFFF)      # the first operands all ones
+    return d, arena, out, 1
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_small_full_products_at_either_word_width(bigint, oracle, bits):
+    """The plan's full products of at most 32 limbs run on 32-bit words (the
+    warp kernel) or on 64-bit limbs (the CTA kernel): the same products."""
+    import torch
+
+    B = bigint
+    d, arena, out_limbs, nflags = _small_mul_batch(B)
+    din = B.to_device(arena)
+    dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
+    dfl = torch.zeros(1, dtype=torch.uint8, device="cuda")
+    plan = B.Plan(d)
+    plan.set_mul_word_bits(bits)
+    assert plan.tuning()["mul_small_word_bits"] == bits
+    plan.execute(din, dout, dfl)
+    torch.cuda.synchronize()
+    check_batch(B, oracle, d, arena, B.to_host(dout, np.uint64), dfl.cpu().numpy())
+    with pytest.raises(B.BigIntError):
+        plan.set_mul_word_bits(48)
+    plan.close()
+
+
+def test_autotune_picks_a_word_width(bigint, oracle):
+    import torch
+
+    B = bigint
+    d, arena, out_limbs, nflags = _small_mul_batch(B, n=900, seed=92)
+    din = B.to_device(arena)
+    dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
+    dfl = torch.zeros(1, dtype=torch.uint8, device="cuda")
+    plan = B.Plan(d)
+    t = plan.autotune(din, dout, dfl, reps=1)
+    assert t["mul_small_word_bits"] in (32, 64) and t == plan.tuning()
+    dout.zero_()
+    plan.execute(din, dout, dfl)
+    torch.cuda.synchronize()
+    check_batch(B, oracle, d, arena, B.to_host(dout, np.uint64), dfl.cpu().numpy())
+    plan.close()
