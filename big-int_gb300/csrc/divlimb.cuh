@@ -84,4 +84,66 @@ __device__ __forceinline__ uint64_t div_2by1(uint64_t u1, uint64_t u0, uint64_t 
     return q1;
 }
 
+// The 3-by-2 reciprocal of a normalised two-limb divisor (d1, d0):
+// v = floor((B^3 - 1) / (d1 B + d0)) - B, from the one-limb reciprocal v of
+// d1 (recip_limb) by Moller and Granlund's Algorithm 6 ("Improved division by
+// invariant integers", IEEE Trans. Computers 60(2), 2011): d1 v + d0 and the
+// high limb of v d0 added up, v stepped down once or twice on each carry.
+// (Checked against floor((B^3 - 1) / D) - B on 5*10^5 random and extreme
+// divisors in a model of this code.)
+__device__ __forceinline__ uint64_t recip_3by2(uint64_t d1, uint64_t d0, uint64_t v) {
+    uint64_t p = d1 * v;
+    p += d0;
+    if (p < d0) {                 // carry
+        v -= 1;
+        if (p >= d1) {
+            v -= 1;
+            p -= d1;
+        }
+        p -= d1;
+    }
+    const uint64_t t0 = v * d0, t1 = __umul64hi(v, d0);
+    p += t1;
+    if (p < t1) {                 // carry
+        v -= 1;
+        if (p > d1 || (p == d1 && t0 >= d0)) v -= 1;
+    }
+    return v;
+}
+
+// The quotient limb floor((u2 B^2 + u1 B + u0) / (d1 B + d0)) for a
+// normalised (d1, d0) with (u2, u1) < (d1, d0), from its 3-by-2 reciprocal v
+// (Moller and Granlund, "Improved division by invariant integers", IEEE
+// Trans. Computers 60(2), 2011, Algorithm 5): two products for the
+// candidate, one remainder check that steps it down (about half the time),
+// one rare check that steps it up.  This is the long division's estimate
+// with Knuth's q-hat * v_(n-2) test built in (TAOCP 4.3.1, step D3): at most
+// one too large for the full divisor.
+__device__ __forceinline__ uint64_t div_3by2(uint64_t u2, uint64_t u1, uint64_t u0, uint64_t d1, uint64_t d0,
+                                             uint64_t v) {
+    // (q1, q0) = v u2 + (u2, u1)
+    uint64_t q0 = v * u2;
+    uint64_t q1 = __umul64hi(v, u2);
+    const uint64_t s = q0 + u1;
+    q1 += u2 + (s < q0 ? 1 : 0);
+    q0 = s;
+    // (r1, r0) = (u1 - q1 d1, u0) - q1 d0 - (d1, d0)  (mod B^2)
+    uint64_t r1 = u1 - q1 * d1;
+    const uint64_t t0 = d0 * q1, t1 = __umul64hi(d0, q1);
+    uint64_t r0 = u0 - t0;
+    r1 = r1 - t1 - (u0 < t0 ? 1 : 0);
+    const uint64_t r0d = r0 - d0;
+    r1 = r1 - d1 - (r0 < d0 ? 1 : 0);
+    r0 = r0d;
+    q1 += 1;
+    if (r1 >= q0) {               // the candidate is one too large
+        q1 -= 1;
+        const uint64_t x = r0 + d0;
+        r1 += d1 + (x < r0 ? 1 : 0);
+        r0 = x;
+    }
+    if (r1 > d1 || (r1 == d1 && r0 >= d0)) q1 += 1;   // one too small (rare)
+    return q1;
+}
+
 }  // namespace bi

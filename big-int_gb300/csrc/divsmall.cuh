@@ -66,6 +66,19 @@ __host__ __device__ inline bool div_small_on_groups(uint32_t MV, uint64_t n, int
     return MV > 8 && MV <= (uint32_t)DIV_THREAD_MAX_MV && n <= (uint64_t)DIV_SMALL_GROUP_PER_SM * (uint64_t)sms;
 }
 
+// The quotient limb estimate of long division: floor((u2 B^2 + u1 B + u0) /
+// (d1 B + d2)) capped at B - 1, from the top three limbs of the running
+// remainder and the top two of the normalised divisor (v3 = recip_3by2(d1,
+// d2, .)).  It is what Knuth's 2-by-1 trial quotient becomes after the
+// q-hat * d2 test (TAOCP 4.3.1, step D3) -- at most one too large -- in one
+// 3-by-2 division; the remainder's invariant keeps (u2, u1) <= (d1, d2), and
+// equality means a quotient of B or more, capped.
+__device__ __forceinline__ uint64_t qhat_3by2(uint64_t u2, uint64_t u1, uint64_t u0, uint64_t d1, uint64_t d2,
+                                              uint64_t v3) {
+    if (u2 > d1 || (u2 == d1 && u1 >= d2)) return ~0ull;
+    return div_3by2(u2, u1, u0, d1, d2, v3);
+}
+
 // One instance: u (MU 64-bit limbs through load_u), v (MV <= MX limbs through
 // load_v); writes MU quotient limbs and MV remainder limbs.  Returns the
 // status: 0, or 1 when v == 0 (then q = r = 0).
@@ -114,33 +127,14 @@ __device__ __forceinline__ uint8_t div_thread(uint32_t MU, uint32_t MV, LoadU lo
         }
     }
     const uint64_t d1 = D[MX - 1], d2 = D[MX - 2];
-    const uint64_t vr = recip_limb(d1);
+    const uint64_t v3 = recip_3by2(d1, d2, recip_limb(d1));
     int tn = (int)MU - MX - 1;   // shifted-dividend limb that enters the window next
     for (int j = (int)MU - K; j >= 0; j--) {
         // the raw limb this step's slide needs, loaded first so that its
         // latency overlaps the step's arithmetic
         const uint64_t lower = j > 0 ? raw(tn - 1) : 0;
         const uint64_t u2 = R[MX], u1 = R[MX - 1], u0 = R[MX - 2];
-        uint64_t qh, rh;
-        bool rh_over = false;
-        if (u2 >= d1) {                        // u2 == d1: q-hat = B - 1, r-hat = u1 + d1
-            qh = ~0ull;
-            rh = u1 + d1;
-            rh_over = rh < u1;
-        } else {
-            qh = div_2by1(u2, u1, d1, vr, rh);
-        }
-        for (int t = 0; t < 2 && !rh_over; t++) {   // q-hat * d2 > r-hat * B + u0: one too large
-            const uint64_t p_lo = qh * d2, p_hi = __umul64hi(qh, d2);
-            if (p_hi > rh || (p_hi == rh && p_lo > u0)) {
-                qh -= 1;
-                const uint64_t nr = rh + d1;
-                rh_over = nr < rh;
-                rh = nr;
-            } else {
-                break;
-            }
-        }
+        uint64_t qh = qhat_3by2(u2, u1, u0, d1, d2, v3);
         // R -= q-hat * D on the carry flag: the high halves one limb up (R[1..MX]),
         // then the low halves (R[0..MX-1], the borrow out taken from R[MX]);
         // the result is negative iff one of the two wrapped
@@ -283,7 +277,7 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
     const uint64_t d1 = __shfl_sync(FULL, D[VPL - 1], 31);
     const uint64_t d2 = VPL >= 2 ? __shfl_sync(FULL, D[VPL >= 2 ? VPL - 2 : 0], 31) : __shfl_sync(FULL, D[0], 30);
     auto Dv = [&](int i) -> uint64_t { return D[i]; };
-    const uint64_t vr = recip_limb(d1);
+    const uint64_t v3 = recip_3by2(d1, d2, recip_limb(d1));
 
     // the shifted dividend: sh(t) = limb t of u 2^s, t in [0, MU]
     auto raw = [&](int t) -> uint64_t { return (t >= 0 && t < (int)MU) ? load_u((uint32_t)t) : 0; };
@@ -308,26 +302,7 @@ __device__ __forceinline__ uint8_t div_warp(uint32_t MU, uint32_t MV, LoadU load
         const uint64_t u2 = rtop;
         const uint64_t u1 = __shfl_sync(FULL, R[VPL - 1], 31);
         const uint64_t u0 = VPL >= 2 ? __shfl_sync(FULL, R[VPL >= 2 ? VPL - 2 : 0], 31) : __shfl_sync(FULL, R[0], 30);
-        uint64_t qh, rh;
-        bool rh_over = false;
-        if (u2 >= d1) {                        // u2 == d1: q-hat = B - 1, r-hat = u1 + d1
-            qh = ~0ull;
-            rh = u1 + d1;
-            rh_over = rh < u1;
-        } else {
-            qh = div_2by1(u2, u1, d1, vr, rh);
-        }
-        for (int t = 0; t < 2 && !rh_over; t++) {   // q-hat * d2 > r-hat * B + u0: one too large
-            const uint64_t p_lo = qh * d2, p_hi = __umul64hi(qh, d2);
-            if (p_hi > rh || (p_hi == rh && p_lo > u0)) {
-                qh -= 1;
-                const uint64_t nr = rh + d1;
-                rh_over = nr < rh;
-                rh = nr;
-            } else {
-                break;
-            }
-        }
+        uint64_t qh = qhat_3by2(u2, u1, u0, d1, d2, v3);
         // pass A: R -= (high halves of q-hat D) shifted up one position, in
         // lane, borrows across lanes resolved by two ballots; the borrow into
         // each lane is applied by pass B's chain
@@ -500,7 +475,8 @@ __device__ __forceinline__ uint8_t div_group(bool valid, uint32_t MU, uint32_t M
     const uint64_t d1 = __shfl_sync(FULL, D[VPL - 1], G - 1, G);
     const uint64_t d2 = VPL >= 2 ? __shfl_sync(FULL, D[VPL >= 2 ? VPL - 2 : 0], G - 1, G)
                                  : __shfl_sync(FULL, D[0], G - 2, G);
-    const uint64_t vr = recip_limb(zero ? (1ull << 63) : d1);
+    const uint64_t d1n = zero ? (1ull << 63) : d1;   // a group without a division gets a normalised stand-in
+    const uint64_t v3 = recip_3by2(d1n, zero ? 0 : d2, recip_limb(d1n));
 
     auto raw = [&](int t) -> uint64_t { return (valid && t >= 0 && t < (int)MU) ? load_u((uint32_t)t) : 0; };
     auto sh = [&](int t) -> uint64_t { return (raw(t) << s) | ((raw(t - 1) >> 1) >> rs); };
@@ -526,28 +502,7 @@ __device__ __forceinline__ uint8_t div_group(bool valid, uint32_t MU, uint32_t M
         const uint64_t u1 = __shfl_sync(FULL, R[VPL - 1], G - 1, G);
         const uint64_t u0 = VPL >= 2 ? __shfl_sync(FULL, R[VPL >= 2 ? VPL - 2 : 0], G - 1, G)
                                      : __shfl_sync(FULL, R[0], G - 2, G);
-        uint64_t qh = 0, rh = 0;
-        if (act) {
-            bool rh_over = false;
-            if (u2 >= d1) {                          // u2 == d1: q-hat = B - 1, r-hat = u1 + d1
-                qh = ~0ull;
-                rh = u1 + d1;
-                rh_over = rh < u1;
-            } else {
-                qh = div_2by1(u2, u1, d1, vr, rh);
-            }
-            for (int t = 0; t < 2 && !rh_over; t++) {   // q-hat * d2 > r-hat * B + u0: one too large
-                const uint64_t p_lo = qh * d2, p_hi = __umul64hi(qh, d2);
-                if (p_hi > rh || (p_hi == rh && p_lo > u0)) {
-                    qh -= 1;
-                    const uint64_t nr = rh + d1;
-                    rh_over = nr < rh;
-                    rh = nr;
-                } else {
-                    break;
-                }
-            }
-        }
+        uint64_t qh = act ? qhat_3by2(u2, u1, u0, d1, d2, v3) : 0;
         // R -= q-hat D in two passes as div_warp (q-hat = 0 leaves R as it is)
         uint64_t coutA, coutB;
         bool neg;
