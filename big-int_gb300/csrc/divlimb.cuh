@@ -89,8 +89,8 @@ __device__ __forceinline__ uint64_t div_2by1(uint64_t u1, uint64_t u0, uint64_t 
 // d1 (recip_limb) by Moller and Granlund's Algorithm 6 ("Improved division by
 // invariant integers", IEEE Trans. Computers 60(2), 2011): d1 v + d0 and the
 // high limb of v d0 added up, v stepped down once or twice on each carry.
-// (Checked against floor((B^3 - 1) / D) - B on 5*10^5 random and extreme
-// divisors in a model of this code.)
+// (A line-for-line model of this code and of div_3by2 is checked against
+// exact division in tests/test_div_estimate_model.py.)
 __device__ __forceinline__ uint64_t recip_3by2(uint64_t d1, uint64_t d0, uint64_t v) {
     uint64_t p = d1 * v;
     p += d0;
