@@ -135,14 +135,14 @@ __device__ __forceinline__ uint64_t div_3by2(uint64_t u2, uint64_t u1, uint64_t 
     const uint64_t r0d = r0 - d0;
     r1 = r1 - d1 - (r0 < d0 ? 1 : 0);
     r0 = r0d;
-    q1 += 1;
-    if (r1 >= q0) {               // the candidate is one too large
-        q1 -= 1;
-        const uint64_t x = r0 + d0;
-        r1 += d1 + (x < r0 ? 1 : 0);
-        r0 = x;
-    }
-    if (r1 > d1 || (r1 == d1 && r0 >= d0)) q1 += 1;   // one too small (rare)
+    // the two adjustments as selects, not branches: the estimate is on every
+    // quotient limb's critical path
+    const bool down = r1 >= q0;   // the candidate q1 + 1 is one too large
+    q1 += down ? 0 : 1;
+    const uint64_t x = r0 + (down ? d0 : 0);
+    r1 += (down ? d1 : 0) + (x < r0 ? 1 : 0);
+    r0 = x;
+    q1 += (r1 > d1 || (r1 == d1 && r0 >= d0)) ? 1 : 0;   // one too small (rare)
     return q1;
 }
 

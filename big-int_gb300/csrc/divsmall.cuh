@@ -75,8 +75,8 @@ __host__ __device__ inline bool div_small_on_groups(uint32_t MV, uint64_t n, int
 // equality means a quotient of B or more, capped.
 __device__ __forceinline__ uint64_t qhat_3by2(uint64_t u2, uint64_t u1, uint64_t u0, uint64_t d1, uint64_t d2,
                                               uint64_t v3) {
-    if (u2 > d1 || (u2 == d1 && u1 >= d2)) return ~0ull;
-    return div_3by2(u2, u1, u0, d1, d2, v3);
+    const uint64_t q = div_3by2(u2, u1, u0, d1, d2, v3);   // plain arithmetic whatever the inputs
+    return (u2 > d1 || (u2 == d1 && u1 >= d2)) ? ~0ull : q;
 }
 
 // One instance: u (MU 64-bit limbs through load_u), v (MV <= MX limbs through

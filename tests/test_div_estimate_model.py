@@ -50,21 +50,19 @@ def div_3by2(u2, u1, u0, d1, d0, v):
     r0d = (r0 - d0) & M
     r1 = (r1 - d1 - (1 if r0 < d0 else 0)) & M
     r0 = r0d
-    q1 = (q1 + 1) & M
-    if r1 >= q0:
-        q1 = (q1 - 1) & M
-        x = (r0 + d0) & M
-        r1 = (r1 + d1 + (1 if x < r0 else 0)) & M
-        r0 = x
+    down = r1 >= q0
+    q1 = (q1 + (0 if down else 1)) & M
+    x = (r0 + (d0 if down else 0)) & M
+    r1 = (r1 + (d1 if down else 0) + (1 if x < r0 else 0)) & M
+    r0 = x
     if r1 > d1 or (r1 == d1 and r0 >= d0):
         q1 += 1
     return q1
 
 
 def qhat_3by2(u2, u1, u0, d1, d2, v3):
-    if u2 > d1 or (u2 == d1 and u1 >= d2):
-        return M
-    return div_3by2(u2, u1, u0, d1, d2, v3)
+    q = div_3by2(u2, u1, u0, d1, d2, v3)
+    return M if (u2 > d1 or (u2 == d1 and u1 >= d2)) else q
 
 
 def _divisors(rng, n):
