@@ -1,7 +1,8 @@
 // divlimb.cuh -- one-limb division helpers shared by the long division
 // (divsmall.cuh), the shifted inverse (divcore.cuh) and the batched division
 // primitives (prims.cu): the reciprocal of a normalised limb and the 2-by-1
-// division that uses it.
+// division that uses it, and the 3-by-2 reciprocal and division that long
+// division's quotient-limb estimate uses.
 #pragma once
 
 #include <stdint.h>

@@ -1,7 +1,7 @@
 // divsmall.cuh -- division of one instance by one thread, for divisors of at
 // most 16 64-bit limbs: schoolbook long division (Knuth, TAOCP vol. 2,
-// 4.3.1, Algorithm D) with 2-by-1 quotient estimates (Moller and Granlund's
-// reciprocal, divlimb.cuh).  The quotient and remainder of u / v are unique,
+// 4.3.1, Algorithm D) with 3-by-2 quotient estimates (Moller and Granlund's
+// reciprocals, divlimb.cuh).  The quotient and remainder of u / v are unique,
 // so the results are the ones the shifted-inverse division (divcore.cuh, the
 // reference's algorithm) gives; what changes is the cost.  Long division does
 // (MU - K + 1) K limb products for a K-limb divisor, about one multiply's
@@ -226,7 +226,7 @@ __device__ __forceinline__ uint64_t warp_chain_in(bool g, bool p, uint64_t& cout
 // long division of div_thread with the divisor and the window spread over
 // the lanes, VPL limbs each (lane l holds positions l VPL .. l VPL + VPL - 1,
 // MX = 32 VPL), the top window limb R[MX] uniform in every lane.  Each
-// quotient limb costs the uniform 2-by-1 estimate, two in-lane borrow chains
+// quotient limb costs the uniform 3-by-2 estimate, two in-lane borrow chains
 // (the high halves of q-hat D, then the low halves) resolved across lanes by
 // two ballots each, and a one-limb slide; the dividend streams in through a
 // 32-limb buffer loaded by the whole warp every 32 quotient limbs.
