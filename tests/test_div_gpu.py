@@ -265,15 +265,18 @@ def test_small_divisors_on_groups_and_threads(bigint, oracle, dtype, mv, n):
     _run(bigint, oracle, u, v, "auto")
 
 
+@pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
 @pytest.mark.parametrize("method", ["auto", "long"])
 @pytest.mark.parametrize("mv,n", [(20, 100), (32, 2000), (50, 300), (64, 2000), (100, 40), (128, 2000)])
-def test_small_batches_on_warps_large_on_groups(bigint, oracle, mv, n, method):
-    """Divisors of 17..128 limbs: up to 10 instances an SM divide on one warp
-    each (div_small_on_warps), more on shared lane groups; the same (q, r)."""
-    u = uniform_limbs(311 + mv + n, n, 2 * mv)
-    v = uniform_limbs(312 + mv + n, n, mv)
-    v[:, -1] |= np.uint64(1)
+def test_small_batches_on_warps_large_on_groups(bigint, oracle, mv, n, method, dtype):
+    """Divisors of 17..128 64-bit limbs: up to 10 instances an SM divide on one
+    warp each (div_small_on_warps), more on shared lane groups; the same (q, r)."""
+    w = 2 if dtype == np.uint32 else 1           # u32 limbs a 64-bit limb
+    u = uniform_limbs(311 + mv + n, n, 2 * mv * w, dtype)
+    v = uniform_limbs(312 + mv + n, n, mv * w, dtype)
+    v[:, -1] |= dtype(1)
+    top = np.iinfo(dtype).max
     for i in range(0, n, 5):                       # all-ones rows: the estimate's q-hat = B - 1 branch
-        v[i, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
-        u[i, :] = np.uint64(0xFFFFFFFFFFFFFFFF)
+        v[i, :] = top
+        u[i, :] = top
     _run(bigint, oracle, u, v, method)
