@@ -308,7 +308,7 @@ def div_method(mv: int, n: int, sms: int) -> str:
         return "long_group" if mv > 8 and n <= 48 * sms else "long_thread"
     if mv <= 64:
         return "long_group"
-    if mv <= 1024 and n > (2 if mv <= 128 else 4 if mv <= 256 else 5 if mv <= 512 else 4) * sms:
+    if mv <= 1024 and n > (2 if mv <= 128 else 3 if mv <= 256 else 5 if mv <= 512 else 4) * sms:
         return "long_group"
     return "shinv"
 

@@ -32,13 +32,13 @@ constexpr int DIV_WARP_CTA = 128;       // threads per CTA of the one-warp-per-i
 // finishes sooner; past a few instances per SM the groups' throughput wins.
 // Measured crossovers (dividend 2 MV limbs, GB300, the shapes div.cu
 // launches): long division always up to 64 limbs (with few instances on one
-// warp each: 152 divisions of 128/64 limbs take 30 us, the shifted inverse
-// 40); above that once n exceeds 2, 4, 5 and 4 instances per SM for divisors
+// warp each: 152 divisions of 128/64 limbs take 29 us, the shifted inverse
+// 40); above that once n exceeds 2, 3, 5 and 4 instances per SM for divisors
 // up to 128, 256, 512 and 1024 limbs.
 __host__ __device__ inline bool div_use_long(uint32_t MV, uint64_t n, int sms) {
     if (MV <= 64) return true;
     if (MV > (uint32_t)DIV_WARP_MAX_MV) return false;
-    const uint64_t per_sm = MV <= 128 ? 2 : MV <= 256 ? 4 : MV <= 512 ? 5 : 4;
+    const uint64_t per_sm = MV <= 128 ? 2 : MV <= 256 ? 3 : MV <= 512 ? 5 : 4;
     return n > per_sm * (uint64_t)sms;
 }
 
