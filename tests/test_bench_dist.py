@@ -75,3 +75,36 @@ def test_gu32ops_follows_the_reference_formula():
     n, words, ms = 4096, 128, 0.5
     assert abs(bench.gu32ops(n, words, ms) - n * 300 * words * 7 / (ms * 1000 * 1000)) < 1e-9
     assert bench.gu32ops(1, 2, 1e-6) == 300 * 2 * 1   # log2(2) = 1
+
+
+def test_bench_division_method_follows_the_library_rule():
+    """bench.div_method (which method's limb products a division rate is
+    counted in) restates div_small_on_groups / div_use_long of divsmall.cuh;
+    the thresholds are read from that header so that the two cannot drift."""
+    import re
+
+    sys.path.insert(0, REPO)
+    import bench
+
+    src = open(os.path.join(REPO, "big-int_gb300", "csrc", "divsmall.cuh")).read()
+    group_per_sm = int(re.search(r"DIV_SMALL_GROUP_PER_SM\s*=\s*(\d+)", src).group(1))
+    thread_max = int(re.search(r"DIV_THREAD_MAX_MV\s*=\s*(\d+)", src).group(1))
+    long_all = int(re.search(r"if \(MV <= (\d+)\) return true;", src).group(1))
+    m = re.search(r"per_sm = MV <= 128 \? (\d+) : MV <= 256 \? (\d+) : MV <= 512 \? (\d+) : (\d+);", src)
+    per_sm = [int(x) for x in m.groups()]
+
+    def rule(mv, n, sms):
+        if mv <= thread_max:
+            return "long_group" if mv > 8 and n <= group_per_sm * sms else "long_thread"
+        if mv <= long_all:
+            return "long_group"
+        if mv <= 1024:
+            k = per_sm[0] if mv <= 128 else per_sm[1] if mv <= 256 else per_sm[2] if mv <= 512 else per_sm[3]
+            if n > k * sms:
+                return "long_group"
+        return "shinv"
+
+    for sms in (152, 148):
+        for mv in (1, 4, 8, 9, 16, 17, 32, 64, 65, 128, 129, 256, 257, 512, 513, 1024, 1025):
+            for n in (1, 100, 300, 456, 457, 608, 609, 760, 761, 912, 913, 1520, 7296, 7297, 20000):
+                assert bench.div_method(mv, n, sms) == rule(mv, n, sms), (mv, n, sms)
