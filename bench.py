@@ -476,10 +476,18 @@ def measure_extra(B, L, stream, args):
             cpu = {"instances_per_s": round(cpu_sample_rate(lambda: O.div_ref(hu, hv, nthreads=th), k)),
                    "threads": th, "sample": f"the first {k} pairs", "kind": "port",
                    "what": "the oracle's restatement of prototypes/div.c div_shinv (u32 digits), all host threads"}
-        div[f"m{mv}_n{n}"] = {"method": method, "instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4), "cpu": cpu,
-                              "word_products_per_div": wp, "word_products_per_s": wp * n / ms * 1e3,
-                              "frac_of_intpipe_peak": round(wp * n / ms * 1e3 / peak_wps, 4),
-                              "shinv_instances_per_s": round(n / ms_shinv * 1e3)}
+        entry = {"method": method, "instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4), "cpu": cpu,
+                 "word_products_per_div": wp, "word_products_per_s": wp * n / ms * 1e3,
+                 "frac_of_intpipe_peak": round(wp * n / ms * 1e3 / peak_wps, 4),
+                 "shinv_instances_per_s": round(n / ms_shinv * 1e3)}
+        if not args.no_cpu:
+            # the reference's own work figure: the word products of div.c's multiplications on this
+            # instance (the first pair), as the instrumented oracle counts them; the rate in that
+            # work can exceed the integer peak because long division does far fewer products
+            divc = O.div_ref_word_products(hu[0], hv[0])
+            entry["divc_word_products_per_div"] = divc
+            entry["intpipe_peak_multiple_in_divc_work"] = round(divc * n / ms * 1e3 / peak_wps, 3)
+        div[f"m{mv}_n{n}"] = entry
         del u, v, q, rr, st
     out["div_u64_2m_by_m"] = div
     out["uneven_batch"] = measure_uneven_batch(B, L, stream)

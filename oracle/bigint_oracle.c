@@ -110,6 +110,17 @@ static int is_zero(const dg* u, int p) {
     return 1;
 }
 
+/* Word products of the division's multiplications, counted as GMP's
+ * mpz_mul does them on the operands' significant digits (the reference's
+ * mult, div.c:184-199, and mpz_mul_ui): the work figure of the division's
+ * roofline, per thread, read by orc_div_ref_word_products_u32. */
+static __thread uint64_t g_div_wp;
+
+static void count_wp(const dg* u, int pu, const dg* v, int pv) {
+    if (is_zero(u, pu) || is_zero(v, pv)) return;
+    g_div_wp += (uint64_t)(top_digit(u, pu) + 1) * (uint64_t)(top_digit(v, pv) + 1);
+}
+
 static int equal(const dg* u, const dg* v, int p) {
     return memcmp(u, v, (size_t)p * sizeof(dg)) == 0;
 }
@@ -146,12 +157,14 @@ static void dsub_abs(const dg* u, const dg* v, dg* w, int p) { (void)sub_one(u, 
  * product; every call site in the reference keeps the product inside p
  * digits, so the reduction never drops a nonzero digit there. */
 static void dmul(const dg* u, const dg* v, dg* w, int p, dg* tmp) {
+    count_wp(u, p, v, p);
     mul_into(u, (uint32_t)p, v, (uint32_t)p, tmp, (uint32_t)p);
     memcpy(w, tmp, (size_t)p * sizeof(dg));
 }
 
 /* w = u * d, single digit, mod B^p (div.c:202-218) */
 static void dmul_digit(const dg* u, dg d, dg* w, int p) {
+    if (d && !is_zero(u, p)) g_div_wp += (uint64_t)(top_digit(u, p) + 1);
     uint64_t c = 0;
     for (int i = 0; i < p; i++) {
         uint64_t t = (uint64_t)u[i] * d + c;
@@ -198,6 +211,7 @@ static int powerdiff(dctx* c, const dg* v, const dg* w, int h, int l, dg* P) {
     } else {
         /* multmod: full product of the low L digits of v and w */
         memset(P, 0, (size_t)p * sizeof(dg));
+        count_wp(v, L, w, L);
         mul_into(v, (uint32_t)L, w, (uint32_t)L, c->mt, (uint32_t)p);
         memcpy(P, c->mt, (size_t)p * sizeof(dg));
         if (!is_zero(P, p)) {
@@ -328,6 +342,7 @@ static void div_one(const dg* u, const dg* v, dg* q, dg* r, uint32_t m, int fait
     memcpy(q, b, m * sizeof(dg));
     /* remainder and the delta correction (div.c:457-463) */
     dg* vq = a;
+    count_wp(v, (int)m, q, (int)m);
     mul_into(v, m, q, m, vq, (uint32_t)p);
     (void)sub_one(u, vq, r, m);
     while (!less_than(r, v, m)) {
@@ -484,6 +499,22 @@ int orc_div_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r, 
 }
 
 /* 1 on a little-endian host (the u64 <-> u32 view above needs it) */
+/* Word products (32x32-bit) of the multiplications the reference's division
+ * performs for one instance -- u and v of m u32 digits, v nonzero, the
+ * reference's single delta step -- counted on significant digits as GMP
+ * multiplies them.  0 for a zero divisor. */
+uint64_t orc_div_ref_word_products_u32(const dg* u, const dg* v, uint32_t m) {
+    if (is_zero(v, (int)m)) return 0;
+    dg* q = (dg*)calloc(m, sizeof(dg));
+    dg* r = (dg*)calloc(m, sizeof(dg));
+    g_div_wp = 0;
+    div_one(u, v, q, r, m, 1);
+    const uint64_t wp = g_div_wp;
+    free(q);
+    free(r);
+    return wp;
+}
+
 int orc_little_endian(void) {
     const uint64_t x = 1;
     return *(const uint8_t*)&x == 1;

@@ -55,6 +55,8 @@ def lib():
             f.restype = I
         L.orc_div_ref_u32.argtypes = [P, P, P, P, P, U32, U32, U64, I]
         L.orc_div_ref_u32.restype = I
+        L.orc_div_ref_word_products_u32.argtypes = [P, P, U32]
+        L.orc_div_ref_word_products_u32.restype = U64
         L.orc_little_endian.restype = I
         if L.orc_little_endian() != 1:
             raise RuntimeError("oracle requires a little-endian host")
@@ -146,6 +148,20 @@ def div_ref(u, v, nthreads: int = 1):
     st = np.zeros(n, dtype=np.uint8)
     lib().orc_div_ref_u32(_p(u), _p(v), _p(q), _p(r), _p(st), mu, mv, n, nthreads)
     return q, r, st
+
+
+def div_ref_word_products(u, v) -> int:
+    """32x32-bit word products of the multiplications the reference's
+    division (div.c's div_shinv, as div_ref runs it) performs on one
+    instance: u a 1-D array of u32 digits (or u64 limbs, read as u32 pairs),
+    v the divisor, zero-extended to u's digits as div.c requires; counted on
+    significant digits as GMP's mpz_mul multiplies them."""
+    u = np.ascontiguousarray(np.asarray(u).reshape(-1)).view(np.uint32)
+    v = np.ascontiguousarray(np.asarray(v).reshape(-1)).view(np.uint32)
+    m = u.shape[0]
+    vp = np.zeros(m, dtype=np.uint32)
+    vp[: v.shape[0]] = v
+    return int(lib().orc_div_ref_word_products_u32(_p(u), _p(vp), m))
 
 
 def ref_div_u32(u, v):

@@ -182,3 +182,31 @@ def test_primitive_restatements_against_python_ints(oracle):
         for x, dd, qq, rr in zip(ints_a, d, q, rem):
             dd = int(dd)
             assert O.to_int(qq) == (x // dd if dd else 0) and int(rr) == (x % dd if dd else 0)
+
+
+def test_division_word_products_count(oracle):
+    """orc_div_ref_word_products_u32 counts the reference division's
+    multiplications on significant digits: zero for a zero divisor; for a
+    one-digit divisor the inverse is a digit division (no product), so the
+    count is sig(u) * sig(floor(B^h / v)) + sig(q) exactly; and it grows
+    with the size."""
+    B = 1 << 32
+    assert oracle.div_ref_word_products(np.arange(1, 9, dtype=np.uint32), np.zeros(8, np.uint32)) == 0
+    rng = np.random.default_rng(7)
+    for m in (4, 9, 16):
+        u = rng.integers(1, 2**32, size=m, dtype=np.uint32)
+        v0 = int(rng.integers(2, 2**32))
+        h = m
+        w = (B ** h) // v0
+        q = _int(u) // v0
+        sig = lambda x: (x.bit_length() + 31) // 32
+        want = h * sig(w) + sig(q)
+        got = oracle.div_ref_word_products(u, np.array([v0], np.uint32))
+        assert got == want, (m, got, want)
+    wp = []
+    for m in (8, 32, 128):
+        u = rng.integers(0, 2**32, size=2 * m, dtype=np.uint32)
+        v = rng.integers(0, 2**32, size=m, dtype=np.uint32)
+        v[-1] |= 1
+        wp.append(oracle.div_ref_word_products(u, v))
+    assert wp[0] < wp[1] < wp[2] and wp[2] > 16 * wp[0]
