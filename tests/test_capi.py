@@ -126,3 +126,11 @@ def test_gmp_word_converters_round_trip(L):
             assert len(back) == 0 if x == 0 else back[-1] != 0        # no leading zero words
     with pytest.raises(B.BigIntError):
         B.limbs_from_words(np.array([1, 2, 3], dtype=np.uint64), 2)   # needs 3 limbs
+
+
+def test_plan_tuning_arguments_checked_on_host(L):
+    t = (ctypes.c_int * 4)()
+    assert L.bi_plan_set_mul_word_bits(None, 32) == 1                 # NULL plan
+    assert L.bi_plan_get_tuning(None, ctypes.cast(t, ctypes.c_void_p)) == 1
+    assert L.bi_plan_set_tuning(None, 4, 2, 1) == 1
+    assert L.bi_plan_autotune(None, None, None, None, 1, None) == 1
