@@ -93,6 +93,71 @@ __device__ __forceinline__ uint32_t chain_sub(uint64_t (&x)[N], const uint64_t (
     }
 }
 
+__device__ __forceinline__ uint32_t chain_add_n(uint64_t (&x)[1], const uint64_t (&y)[1], uint32_t c) {
+    uint32_t co;
+    asm("{\n\t.reg .u32 t;\n\tadd.cc.u32 t, %3, 0xFFFFFFFF;\n\taddc.cc.u64 %0, %0, %2;\n\taddc.u32 %1, 0, 0;\n\t}"
+        : "+l"(x[0]), "=r"(co)
+        : "l"(y[0]), "r"(c));
+    return co;
+}
+__device__ __forceinline__ uint32_t chain_add_n(uint64_t (&x)[2], const uint64_t (&y)[2], uint32_t c) {
+    uint32_t co;
+    asm("{\n\t.reg .u32 t;\n\tadd.cc.u32 t, %5, 0xFFFFFFFF;\n\taddc.cc.u64 %0, %0, %3;\n\taddc.cc.u64 %1, %1, %4;\n\t"
+        "addc.u32 %2, 0, 0;\n\t}"
+        : "+l"(x[0]), "+l"(x[1]), "=r"(co)
+        : "l"(y[0]), "l"(y[1]), "r"(c));
+    return co;
+}
+__device__ __forceinline__ uint32_t chain_add_n(uint64_t (&x)[4], const uint64_t (&y)[4], uint32_t c) {
+    uint32_t co;
+    asm("{\n\t.reg .u32 t;\n\tadd.cc.u32 t, %9, 0xFFFFFFFF;\n\taddc.cc.u64 %0, %0, %5;\n\taddc.cc.u64 %1, %1, %6;\n\t"
+        "addc.cc.u64 %2, %2, %7;\n\taddc.cc.u64 %3, %3, %8;\n\taddc.u32 %4, 0, 0;\n\t}"
+        : "+l"(x[0]), "+l"(x[1]), "+l"(x[2]), "+l"(x[3]), "=r"(co)
+        : "l"(y[0]), "l"(y[1]), "l"(y[2]), "l"(y[3]), "r"(c));
+    return co;
+}
+template <int N>
+__device__ __forceinline__ uint32_t chain_add(uint64_t (&x)[N], const uint64_t (&y)[N], uint32_t c) {
+    if constexpr (N == 1 || N == 2 || N == 4) {
+        return chain_add_n(x, y, c);
+    } else {
+        static_assert(N % 8 == 0, "chain_add: N must be 1, 2, 4 or a multiple of 8");
+#pragma unroll
+        for (int b = 0; b < N / 8; b++)
+            c = chain_add8(*reinterpret_cast<uint64_t(*)[8]>(&x[8 * b]),
+                           *reinterpret_cast<const uint64_t(*)[8]>(&y[8 * b]), c);
+        return c;
+    }
+}
+
+// x[0..N-1] -= (gen(OFF), gen(OFF + 1), ...) + c, for any N >= 1: blocks of 8
+// limbs, then one of 4, 2 and 1 for the rest, each an asm chain, the borrow
+// handed from block to block.  Returns the borrow out.
+template <int N, int OFF = 0, typename Gen>
+__device__ __forceinline__ uint32_t chain_sub_gen(uint64_t* x, Gen gen, uint32_t c) {
+    static_assert(N >= 1, "chain_sub_gen: N >= 1");
+    constexpr int Bk = N >= 8 ? 8 : N >= 4 ? 4 : N >= 2 ? 2 : 1;
+    uint64_t y[Bk];
+#pragma unroll
+    for (int j = 0; j < Bk; j++) y[j] = gen(OFF + j);
+    c = chain_sub<Bk>(*reinterpret_cast<uint64_t(*)[Bk]>(x), y, c);
+    if constexpr (N > Bk) c = chain_sub_gen<N - Bk, OFF + Bk>(x + Bk, gen, c);
+    return c;
+}
+
+// x[0..N-1] += (gen(OFF), gen(OFF + 1), ...) + c, for any N >= 1; returns the carry out.
+template <int N, int OFF = 0, typename Gen>
+__device__ __forceinline__ uint32_t chain_add_gen(uint64_t* x, Gen gen, uint32_t c) {
+    static_assert(N >= 1, "chain_add_gen: N >= 1");
+    constexpr int Bk = N >= 8 ? 8 : N >= 4 ? 4 : N >= 2 ? 2 : 1;
+    uint64_t y[Bk];
+#pragma unroll
+    for (int j = 0; j < Bk; j++) y[j] = gen(OFF + j);
+    c = chain_add<Bk>(*reinterpret_cast<uint64_t(*)[Bk]>(x), y, c);
+    if constexpr (N > Bk) c = chain_add_gen<N - Bk, OFF + Bk>(x + Bk, gen, c);
+    return c;
+}
+
 // x = x - (gen(0), gen(1), ...) - c over N limbs, the subtrahend produced
 // eight limbs at a time just before its chain block, so that no more than
 // eight of its limbs are live at once.

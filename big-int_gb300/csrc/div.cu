@@ -31,6 +31,7 @@
 // DIV_WARP_MAX_MV, where its K (MU - K + 1) limb products and no barriers
 // cost less than a CTA running the steps above (div_use_long holds the
 // measured crossover, which depends on the batch size too).
+#include "divblock.cuh"
 #include "divcore.cuh"
 #include "divsmall.cuh"
 
@@ -195,8 +196,56 @@ static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status,
     else div_warp_kernel<T, 32><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
 }
 
-constexpr uint32_t DIV_MAX_MU64 = 2048;
-constexpr int DIV_AUTO = 0, DIV_SHINV = 1, DIV_LONG = 2;   // method of div_entry   // dividend limbs (u64 view) per instance
+// One instance on NW warps: long division KB quotient limbs at a time
+// (divblock.cuh) for divisors of at most 32 NW VPL limbs.  NW = 1: four
+// warps a CTA, one instance each; NW > 1: one instance a CTA of NW warps.
+template <typename T, int VPL, int KB, int NW>
+__global__ void __launch_bounds__(NW == 1 ? DIV_WARP_CTA : 32 * NW)
+div_blk_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
+               uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
+    __shared__ DivBlkShared<KB, NW> sh;
+    const uint32_t MU = sizeof(T) == 8 ? mu : (mu + 1) / 2, MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    const uint64_t per_cta = NW == 1 ? DIV_WARP_CTA / 32 : 1;
+    const uint64_t stride = (uint64_t)gridDim.x * per_cta;
+    for (uint64_t inst = (uint64_t)blockIdx.x * per_cta + (NW == 1 ? threadIdx.x / 32 : 0); inst < n;
+         inst += stride) {
+        const T* ui = u + inst * mu;
+        const T* vi = v + inst * mv;
+        T* qi = q + inst * mu;
+        T* ri = r + inst * mv;
+        const uint8_t st = div_blk<VPL, KB, NW>(
+            MU, MV, [&](uint32_t i) { return limb64(ui, mu, i); }, [&](uint32_t i) { return limb64(vi, mv, i); },
+            [&](uint32_t i, uint64_t x) { put_limb64(qi, mu, i, x); },
+            [&](uint32_t i, uint64_t x) { put_limb64(ri, mv, i, x); }, &sh);
+        if (status && threadIdx.x % (32 * NW) == 0) status[inst] = st;
+    }
+}
+
+template <typename T, int VPL, int KB, int NW>
+static void launch_blk(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
+                       cudaStream_t s) {
+    const uint64_t per_cta = NW == 1 ? DIV_WARP_CTA / 32 : 1;
+    const uint64_t blocks = (n + per_cta - 1) / per_cta;
+    const unsigned grid = (unsigned)(blocks < (1u << 20) ? blocks : (1u << 20));
+    div_blk_kernel<T, VPL, KB, NW><<<grid, NW == 1 ? DIV_WARP_CTA : 32 * NW, 0, s>>>(u, v, q, r, status, n, mu, mv);
+}
+
+// Long division of divisors of 129..DIV_LONG_MAX_MV limbs, KB quotient limbs
+// at a time (divblock.cuh).
+template <typename T>
+static void launch_div_blk(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
+                           uint64_t n, cudaStream_t s) {
+    const uint32_t MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
+    if (MV <= 256) launch_blk<T, 8, 4, 1>(u, v, q, r, status, mu, mv, n, s);
+    else if (MV <= 512) launch_blk<T, 16, 8, 1>(u, v, q, r, status, mu, mv, n, s);
+    else if (MV <= 1024) launch_blk<T, 32, 8, 1>(u, v, q, r, status, mu, mv, n, s);
+    else if (MV <= 2048) launch_blk<T, 32, 8, 2>(u, v, q, r, status, mu, mv, n, s);
+    else launch_blk<T, 32, 8, 4>(u, v, q, r, status, mu, mv, n, s);
+}
+
+// dividend limbs (u64 view) per instance: any long division, and the shifted inverse's limit
+constexpr uint32_t DIV_MAX_MU64 = 8192, DIV_SHINV_MAX_MU64 = 2048;
+constexpr int DIV_AUTO = 0, DIV_SHINV = 1, DIV_LONG = 2;   // method of div_entry
 
 template <typename T>
 static bi_status div_entry(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
@@ -209,18 +258,27 @@ static bi_status div_entry(const T* u, const T* v, T* q, T* r, uint8_t* status, 
         (uintptr_t)r % sizeof(T))
         return set_error(BI_EINVAL, "buffers must be aligned to the limb size");
     const DivGeom g = div_geom(mu, mv, (int)sizeof(T));
-    if (method == DIV_LONG && g.MV > (uint32_t)DIV_WARP_MAX_MV)
-        return set_error(BI_EUNSUPPORTED, "div_long: divisor of %u limbs above %d 64-bit limbs", mv, DIV_WARP_MAX_MV);
+    if (g.MU > DIV_MAX_MU64) return set_error(BI_EUNSUPPORTED, "div: dividend of %u limbs above the supported size", mu);
+    if (method == DIV_LONG && g.MV > (uint32_t)DIV_LONG_MAX_MV)
+        return set_error(BI_EUNSUPPORTED, "div_long: divisor of %u limbs above %d 64-bit limbs", mv, DIV_LONG_MAX_MV);
+    if (method == DIV_SHINV && g.MU > DIV_SHINV_MAX_MU64)
+        return set_error(BI_EUNSUPPORTED, "div_shinv: dividend of %u limbs above %u 64-bit limbs", mu,
+                         DIV_SHINV_MAX_MU64);
     if (method != DIV_SHINV && g.MV <= (uint32_t)DIV_THREAD_MAX_MV) {
         launch_div_thread(u, v, q, r, status, mu, mv, n, (cudaStream_t)s);
         return check_launch("div thread kernel");
     }
-    if (method != DIV_SHINV && g.MV <= (uint32_t)DIV_WARP_MAX_MV &&
-        (method == DIV_LONG || div_use_long(g.MV, n, num_sms()))) {
-        launch_div_warp(u, v, q, r, status, mu, mv, n, (cudaStream_t)s);
-        return check_launch("div warp kernel");
+    // the shifted inverse holds its operands in shared memory: dividends above
+    // DIV_SHINV_MAX_MU64 limbs always take long division
+    if (method != DIV_SHINV && g.MV <= (uint32_t)DIV_LONG_MAX_MV &&
+        (method == DIV_LONG || g.MU > DIV_SHINV_MAX_MU64 || div_use_long(g.MV, n, num_sms()))) {
+        if (g.MV <= 128) {
+            launch_div_warp(u, v, q, r, status, mu, mv, n, (cudaStream_t)s);
+            return check_launch("div warp kernel");
+        }
+        launch_div_blk(u, v, q, r, status, mu, mv, n, (cudaStream_t)s);
+        return check_launch("div block kernel");
     }
-    if (g.MU > DIV_MAX_MU64) return set_error(BI_EUNSUPPORTED, "div: dividend of %u limbs above the supported size", mu);
     const size_t smem = div_smem_bytes(g);
     if (smem > 227 * 1024) return set_error(BI_EUNSUPPORTED, "div: sizes need too much shared memory");
     const int threads = div_threads(g.MU);

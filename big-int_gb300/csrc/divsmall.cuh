@@ -25,6 +25,7 @@ constexpr int DIV_THREAD_MAX_MV = 16;   // 64-bit divisor limbs handled by div_t
 constexpr int DIV_THREAD_CTA = 64;      // threads per CTA of the one-thread-per-instance kernels
 constexpr int DIV_WARP_MAX_MV = 1024;   // 64-bit divisor limbs handled by div_warp
 constexpr int DIV_WARP_CTA = 128;       // threads per CTA of the one-warp-per-instance kernels
+constexpr int DIV_LONG_MAX_MV = 4096;   // 64-bit divisor limbs handled by long division (divblock.cuh above 128)
 // Long division on lane groups or the shifted inverse on CTAs, for a batch
 // of n instances with MV-limb divisors (64-bit limbs) on a GPU of `sms` SMs.
 // Long division does fewer limb products but runs one quotient limb after
@@ -37,7 +38,7 @@ constexpr int DIV_WARP_CTA = 128;       // threads per CTA of the one-warp-per-i
 // up to 128, 256, 512 and 1024 limbs.
 __host__ __device__ inline bool div_use_long(uint32_t MV, uint64_t n, int sms) {
     if (MV <= 64) return true;
-    if (MV > (uint32_t)DIV_WARP_MAX_MV) return false;
+    if (MV > (uint32_t)DIV_WARP_MAX_MV) return MV <= (uint32_t)DIV_LONG_MAX_MV;
     const uint64_t per_sm = MV <= 128 ? 2 : MV <= 256 ? 3 : MV <= 512 ? 5 : 4;
     return n > per_sm * (uint64_t)sms;
 }

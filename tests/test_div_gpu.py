@@ -115,8 +115,9 @@ def test_large_divisions(bigint, oracle, mv, method):
 
 @pytest.mark.parametrize("mu,mv", [(16, 16), (17, 17), (40, 32), (40, 33), (2048, 1024), (2048, 1025), (2048, 2048)])
 def test_method_boundaries(bigint, oracle, mu, mv):
-    """Divisor sizes on either side of the long-division limits (16 and 1024
-    64-bit limbs) and the largest supported dividend, by both methods."""
+    """Divisor sizes on either side of the method limits (16 and 128 64-bit
+    limbs for the thread and warp long divisions) and the shifted inverse's
+    largest dividend, by every method."""
     n = 3
     u = uniform_limbs(311 + mv, n, mu)
     v = uniform_limbs(312 + mv, n, mv)
@@ -124,11 +125,21 @@ def test_method_boundaries(bigint, oracle, mu, mv):
     v[1, mv // 2:] = 0                 # shorter divisor in a wider row
     v[1, mv // 2 - 1] |= 1
     for method in ("auto", "shinv", "long"):
-        if method == "long" and mv > 1024:
-            with pytest.raises(bigint.BigIntError):
-                _run(bigint, oracle, u, v, method)
-        else:
-            _run(bigint, oracle, u, v, method)
+        _run(bigint, oracle, u, v, method)
+
+
+def test_size_limits_rejected(bigint):
+    """Dividends above 8192 64-bit limbs, shifted-inverse dividends above 2048
+    and long-division divisors above 4096 are refused before any launch."""
+    import torch
+
+    B = bigint
+    for mu, mv, method in [(8193, 4, "auto"), (2049, 1000, "shinv"), (8192, 4097, "long")]:
+        u = torch.zeros((1, mu), dtype=torch.int64, device="cuda")
+        v = torch.ones((1, mv), dtype=torch.int64, device="cuda")
+        with pytest.raises(B.BigIntError) as ei:
+            B.div(u, v, method=method)
+        assert ei.value.status == 6            # BI_EUNSUPPORTED
 
 
 @pytest.mark.parametrize("method", ["auto", "long", "shinv"])
