@@ -3,11 +3,11 @@
 # into baseline/_ref/cuda/ so the reference kernels can be compiled on the
 # GPU machine, where the reference checkout does not exist.  baseline/_ref/ is
 # git-ignored: nothing of the reference enters the repository's history.
+# Usage: REF=<reference checkout> sh install_ref.sh
 set -e
-REF=${REF:-/root/reference}
 HERE=$(cd "$(dirname "$0")" && pwd)
-if [ ! -f "$REF/cuda/ker-mul.cu.h" ]; then
-    echo "reference checkout not found at $REF; nothing staged"
+if [ -z "${REF:-}" ] || [ ! -f "$REF/cuda/ker-mul.cu.h" ]; then
+    echo "REF does not name a reference checkout with cuda/ker-mul.cu.h; nothing staged"
     exit 0
 fi
 mkdir -p "$HERE/_ref/cuda"

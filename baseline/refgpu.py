@@ -20,9 +20,21 @@ SRC = os.path.join(HERE, "ref_gpu.cu")
 _lib = None
 
 
+def reference_checkout():
+    """The reference checkout: $BIGINT_REF, else a `reference` directory
+    beside the repository; None when neither exists (as on a GPU machine)."""
+    for cand in (os.environ.get("BIGINT_REF"), os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")):
+        if cand and os.path.isdir(cand):
+            return cand
+    return None
+
+
 def build() -> bool:
     """Stage the reference headers (when the checkout exists) and compile."""
-    subprocess.run(["sh", os.path.join(HERE, "install_ref.sh")], capture_output=True)
+    ref = reference_checkout()
+    if ref:
+        subprocess.run(["sh", os.path.join(HERE, "install_ref.sh")], capture_output=True,
+                       env=dict(os.environ, REF=ref))
     if not os.path.exists(HDR):
         return False
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(HDR)):

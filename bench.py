@@ -265,18 +265,20 @@ def run_reference(args) -> None:
 
     O.build()
     cores = os.cpu_count() or 1
-    sample_limbs = 1 << (args.total_limbs_log2 - 3)
-    data = {(bits, op): addsub_u64(bits, seed=SEED_ADDSUB, total_limbs=sample_limbs, op=op)
-            for bits in BITS for op in ("add", "sub")}
-    per_step = sum(3 * a.size * 8 + (a.shape[0] if op == "sub" else 0) for (bits, op), (a, b) in data.items())
-    for _ in range(args.warmup):
-        for (bits, op), (a, b) in data.items():
-            cpu_addsub(op, a, b, cores)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        for (bits, op), (a, b) in data.items():
-            cpu_addsub(op, a, b, cores)
-    wall = time.perf_counter() - t0
+    total = 1 << args.total_limbs_log2
+    # the full workload, one (size, op) at a time so that host memory holds
+    # one pair of 2^27-limb operands: generate (untimed), warm up, time K steps
+    per_step = 0
+    wall = 0.0
+    for bits in BITS:
+        for op in ("add", "sub"):
+            a, b = addsub_u64(bits, seed=SEED_ADDSUB, total_limbs=total, op=op)
+            per_step += 3 * a.size * 8 + (a.shape[0] if op == "sub" else 0)
+            for _ in range(args.warmup):
+                cpu_addsub(op, a, b, cores)
+            for _ in range(args.steps):
+                wall += cpu_addsub(op, a, b, cores)
+            del a, b
     v = per_step * args.steps / wall / 1e9
     line = {
         "impl": "reference",
@@ -285,10 +287,11 @@ def run_reference(args) -> None:
         "warmup": args.warmup, "ms_per_step": round(1000 * wall / max(1, args.steps), 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
         "data": "synthetic (splitmix64 seed 1001; 20% carry-chain instances)",
-        "config": {"workload": "addsub_u64 sweep: 9 sizes 2^10..2^18 bits x {add, sub}",
-                   "sample": f"2^{args.total_limbs_log2 - 3} limbs per operand per size (1/8 of the GPU workload)"},
+        "config": {"workload": "addsub_u64 sweep: 9 sizes 2^10..2^18 bits x {add, sub}, n = 2^27/m instances per size",
+                   "sample": f"the full workload: 2^{args.total_limbs_log2} limbs per operand per size",
+                   "same_config": args.total_limbs_log2 == 27},
         "cpu_baseline": {"value": round(v, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-                         "sample": "each step: the 9-size add+sub sweep at 1/8 of the GPU workload's limbs; "
+                         "sample": "each step: the 9-size add+sub sweep at the GPU workload's full size; "
                                    "the oracle port of ker-add.cu.h / sub.fut, one pthread per core"},
         "e2e": {"value": round(v, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -490,7 +493,7 @@ def measure_extra(B, L, stream, args):
         div[f"m{mv}_n{n}"] = entry
         del u, v, q, rr, st
     out["div_u64_2m_by_m"] = div
-    out["uneven_batch"] = measure_uneven_batch(B, L, stream)
+    out["uneven_batch"] = measure_uneven_batch(B, L, stream, peak_wps=peak_wps)
     out["reference_cuda_kernels"] = measure_reference_kernels(B, L, stream)
     out["chains"] = measure_chains(B, L, stream)
     out["serving"] = measure_serving(B)
@@ -498,7 +501,7 @@ def measure_extra(B, L, stream, args):
     return out
 
 
-def measure_uneven_batch(B, L, stream, n: int = 100_000):
+def measure_uneven_batch(B, L, stream, n: int = 100_000, peak_wps: float = 0.0):
     """100k mixed instances (sizes log-uniform 256..65536 bits; 20% add, 20% sub,
     40% full multiply, 20% division): one graph-captured plan launch versus the
     plain one-launch-per-(op, size) kernels on the same instances."""
@@ -509,7 +512,7 @@ def measure_uneven_batch(B, L, stream, n: int = 100_000):
     dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
     dfl = torch.zeros(nflags, dtype=torch.uint8, device="cuda")
     t0 = time.perf_counter()
-    plan = B.Plan(d)
+    plan = B.Plan(d, len(arena), out_limbs, nflags)
     plan_ms = (time.perf_counter() - t0) * 1e3
     chosen = plan.autotune(din, dout, dfl, reps=2)
     ms_batch = event_time(stream, lambda: plan.execute(din, dout, dfl, stream=stream), 5, 2)
@@ -535,28 +538,53 @@ def measure_uneven_batch(B, L, stream, n: int = 100_000):
             calls.append((op, a, b, (torch.empty_like(a), torch.empty_like(b)),
                           torch.empty(g, dtype=torch.uint8, device="cuda"), m, mb, g))
 
-    def per_size():
+    def per_size_on(s_):
         for op, a, b, r, s, m, mb, g in calls:
             if op == B.OP_ADD:
-                check(L, L.bi_add_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, g, sp))
+                check(L, L.bi_add_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, g, s_))
             elif op == B.OP_SUB:
-                check(L, L.bi_sub_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), s.data_ptr(), m, g, sp))
+                check(L, L.bi_sub_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), s.data_ptr(), m, g, s_))
             elif op == B.OP_MULFULL:
-                check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, g, sp))
+                check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, g, s_))
             else:
                 check(L, L.bi_div_u64(a.data_ptr(), b.data_ptr(), r[0].data_ptr(), r[1].data_ptr(), s.data_ptr(),
-                                      m, mb, g, sp))
+                                      m, mb, g, s_))
 
-    ms_per_size = event_time(stream, per_size, 2, 1)
+    ms_per_size = event_time(stream, lambda: per_size_on(sp), 2, 1)
+    # the same launches captured once into a CUDA graph and replayed: the
+    # per-size baseline without the host's per-call overhead
+    ms_per_size_graph = graph_time(per_size_on, reps=1)
     st = plan.stats()
     plan.close()
+    # the batch's algorithmic work: word products of the full multiplies (4 m^2)
+    # and of long division ((m - mb + 1) mb limb products, 4 words each), and the
+    # bytes of add/sub (read a, b, write r; + 1 sign byte for sub)
+    ops, ms_, mbs = d["op"].astype(np.int64), d["m"].astype(np.int64), d["mb"].astype(np.int64)
+    wp = int((4 * ms_ * ms_)[ops == B.OP_MULFULL].sum() + (4 * ms_ * ms_)[ops == B.OP_MUL].sum() // 2
+             + (4 * (ms_ - mbs + 1) * mbs)[ops == B.OP_DIV].sum())
+    ab = int((24 * ms_)[ops == B.OP_ADD].sum() + (24 * ms_ + 1)[ops == B.OP_SUB].sum())
+    ipeak = peak_wps or max(B.probe_intpipe().values())
+    hpeak, _ = measured_peaks()
+    f_int = wp / (ms_batch / 1e3) / ipeak
+    f_hbm = ab / (ms_batch / 1e3) / 1e9 / hpeak
     del din, dout, dfl, calls
     torch.cuda.empty_cache()
     return {"instances": n, "batched_inst_per_s": round(n / ms_batch * 1e3), "batched_ms": round(ms_batch, 3),
             "per_size_launch_inst_per_s": round(n / ms_per_size * 1e3), "per_size_launch_ms": round(ms_per_size, 3),
-            "speedup_vs_per_size_launch": round(ms_per_size / ms_batch, 2), "per_size_launches": len(groups),
+            "per_size_graph_inst_per_s": round(n / ms_per_size_graph * 1e3),
+            "per_size_graph_ms": round(ms_per_size_graph, 3),
+            "speedup_vs_per_size_launch": round(ms_per_size / ms_batch, 2),
+            "speedup_vs_per_size_graph": round(ms_per_size_graph / ms_batch, 2),
+            "per_size_launches": len(groups),
+            "roofline": {"word_products": wp, "addsub_bytes": ab,
+                         "word_products_per_s": wp / (ms_batch / 1e3), "frac_of_intpipe_peak": round(f_int, 4),
+                         "addsub_gbs": round(ab / (ms_batch / 1e3) / 1e9, 1), "frac_of_hbm_peak": round(f_hbm, 4),
+                         "sum_of_fracs": round(f_int + f_hbm, 4),
+                         "note": "the batch's kernels share the GPU: the two fractions of the one replay time add up "
+                                 "to the share of the machine's integer-pipe and HBM peaks the batch uses"},
             "plan_create_ms": round(plan_ms, 1), "autotune": chosen, "plan": st,
-            "note": "one CUDA-graph replay of three concurrent persistent kernels vs one plain launch per (op, m) group"}
+            "note": "one CUDA-graph replay of the plan's concurrent persistent kernels vs one plain launch per "
+                    "(op, m) group, issued from Python and as one replay of those launches captured in a CUDA graph"}
 
 
 def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100_000, streams: int = 4,
@@ -822,7 +850,7 @@ def run_single(args) -> None:
         din = B.to_device(arena)
         dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
         dfl = torch.zeros(nflags, dtype=torch.uint8, device="cuda")
-        plan = B.Plan(d)
+        plan = B.Plan(d, len(arena), out_limbs, nflags)
         ms = event_time(stream, lambda: plan.execute(din, dout, dfl, stream=stream), args.steps, args.warmup)
         plan.close()
         print(json.dumps({"workload": w, "n": args.batch_n, "ms": ms, "instances_per_s": args.batch_n / ms * 1e3}))
@@ -831,6 +859,48 @@ def run_single(args) -> None:
         print(json.dumps({"workload": w, "serving": measure_serving(B, rates=rates)}))
     else:
         raise SystemExit(f"unknown workload {w}")
+
+
+def summary(extra, achieved_gbs: float, peak_gbs: float):
+    """The headline results of every workload in a few hundred bytes, the last
+    key of the JSON line: per size the instances/s and fraction of the
+    measured peak, and the ratios against the reference's own kernels."""
+    if not extra:
+        return None
+    sm = {"addsub_sweep_frac_of_hbm_peak": round(achieved_gbs / peak_gbs, 3)}
+    mu = extra.get("mul_u64_full", {})
+    sm["mulfull_u64"] = {k.split("_")[0]: [v["full_instances_per_s"], v["frac_of_intpipe_peak"],
+                                           v["truncated_instances_per_s"]] for k, v in mu.items()}
+    sm["mulfull_u64_fields"] = "m: [full inst/s, full frac of int-pipe peak, truncated inst/s]"
+    dv = extra.get("div_u64_2m_by_m", {})
+    sm["div_u64_2m_by_m"] = {k.split("_")[0]: [v["instances_per_s"], v["frac_of_intpipe_peak"]] for k, v in dv.items()}
+    sm["div_fields"] = "m: [div/s, frac of int-pipe peak in the method's own limb products]"
+    if "mul2048_u32" in extra:
+        sm["c1_mulfull_u32_2048bit_inst_per_s"] = extra["mul2048_u32"]["instances_per_s"]
+    ub = extra.get("uneven_batch")
+    if ub:
+        sm["uneven_batch_100k"] = {"inst_per_s": ub["batched_inst_per_s"],
+                                   "x_per_size_python": ub["speedup_vs_per_size_launch"],
+                                   "x_per_size_graph": ub.get("speedup_vs_per_size_graph"),
+                                   "frac_intpipe": ub.get("roofline", {}).get("frac_of_intpipe_peak"),
+                                   "frac_hbm": ub.get("roofline", {}).get("frac_of_hbm_peak")}
+    rk = extra.get("reference_cuda_kernels", {})
+    if "add_u64_gbs" in rk:
+        sm["x_vs_ref_baddKer3_add"] = {b: round(v["ours"] / v["reference_baddKer3"], 2)
+                                       for b, v in rk["add_u64_gbs"].items() if v.get("reference_baddKer3")}
+    if "mul_u64" in rk:
+        sm["x_vs_ref_convMul5"] = {k.split("_")[0]: {
+            "truncated": round(v["truncated_ours_inst_per_s"] / v["truncated_reference_inst_per_s"], 2),
+            "full": (round(v["full_ours_inst_per_s"] / v["full_reference_inst_per_s"], 2)
+                     if v.get("full_reference_inst_per_s") else None)} for k, v in rk["mul_u64"].items()}
+    if rk.get("mul2048_u32_full_reference_inst_per_s") and "mul2048_u32" in extra:
+        sm["x_vs_ref_convMul5_c1"] = round(extra["mul2048_u32"]["instances_per_s"]
+                                           / rk["mul2048_u32_full_reference_inst_per_s"], 2)
+    sv = extra.get("serving", {}).get("rates_rps", {})
+    sm["serve"] = {r: {"loop_p50_p99_us": [v["loop"]["p50_us"], v["loop"]["p99_us"]],
+                       "launch_p99_us": v["per_request_launch"]["p99_us"],
+                       "achieved_rps": v["loop"]["achieved_rps"]} for r, v in sv.items()}
+    return sm
 
 
 def run_ours(args) -> None:
@@ -997,6 +1067,9 @@ def run_ours(args) -> None:
                          "frac": round(achieved / peak, 4),
                          "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
                          else "of fallback 6.8 TB/s",
+                         "peak_note": "the denominator is a device-to-device copy (one byte read per byte written); "
+                                      "add/sub reads two bytes per byte written, so a streaming kernel can read a "
+                                      "little above 1.0 of it",
                          "kernel": "addsub_chunk_kernel (add and sub launches)", "bytes_per_launch": int(bytes_per_launch),
                          "avg_launch_ms": round(avg_launch_ms, 5),
                          "traffic": (ncu_traffic("addsub_chunk_kernel") or {}).get("bytes_per_launch"),
@@ -1010,6 +1083,7 @@ def run_ours(args) -> None:
                 "sample": f"the full sweep (same inputs, 2^27 limbs per size) run {cpu_reps}x: {cpu_s:.2f} s wall "
                           f"on {nthreads} threads; oracle port of ker-add.cu.h / sub.fut"},
             "extra": extra,
+            "summary": summary(extra, achieved, peak),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -109,7 +109,7 @@ SIGNATURES: dict[str, list] = {
     "bi_host_div_u32": [_P, _P, _P, _P, _P, _U32, _U32, _U64],
     "bi_max_limbs_div_u64": [],
     "bi_max_limbs_div_u32": [],
-    "bi_plan_create": [_P, _P, _U64],
+    "bi_plan_create": [_P, _P, _U64, _U64, _U64, _U64],
     "bi_plan_execute": [_P, _P, _P, _P, _P],
     "bi_plan_autotune": [_P, _P, _P, _P, _I, _P],
     "bi_plan_set_tuning": [_P, _I, _I, _I],
@@ -118,7 +118,7 @@ SIGNATURES: dict[str, list] = {
     "bi_plan_stats": [_P, _P],
     "bi_plan_destroy": [_P],
     "bi_batch_noalloc_max_descs": [],
-    "bi_batch_run_noalloc": [_P, _U64, _P, _P, _P, _P],
+    "bi_batch_run_noalloc": [_P, _U64, _P, _U64, _P, _U64, _P, _U64, _P],
     "bi_probe_intpipe": [_P, _P],
     "bi_add_chain_u64": [_P, _P, _P, _U32, _U64, _U32, _P],
     "bi_add_chain_u32": [_P, _P, _P, _U32, _U64, _U32, _P],
@@ -446,13 +446,19 @@ DESC_DTYPE = np.dtype([("op", "<u4"), ("m", "<u4"), ("mb", "<u4"), ("reserved", 
 
 
 class Plan:
-    """A bucketed, graph-captured execution plan for an uneven batch."""
+    """A bucketed, graph-captured execution plan for an uneven batch.
 
-    def __init__(self, descs: np.ndarray):
+    in_limbs, out_limbs and nflags are the sizes of the input arena, the
+    output arena (64-bit limbs) and the flag arena (bytes) the plan will run
+    on; every descriptor is checked against them when the plan is built
+    (nflags = 0: the plan writes no flags and execute takes flags=None)."""
+
+    def __init__(self, descs: np.ndarray, in_limbs: int, out_limbs: int, nflags: int = 0):
         descs = np.ascontiguousarray(descs, dtype=DESC_DTYPE)
         self.count = len(descs)
         self._h = ctypes.c_void_p()
-        _check(lib().bi_plan_create(ctypes.byref(self._h), descs.ctypes.data_as(ctypes.c_void_p), self.count))
+        _check(lib().bi_plan_create(ctypes.byref(self._h), descs.ctypes.data_as(ctypes.c_void_p), self.count,
+                                    int(in_limbs), int(out_limbs), int(nflags)))
 
     def execute(self, arena_in, arena_out, flags=None, stream=None):
         _check(lib().bi_plan_execute(self._h, arena_in.data_ptr(), arena_out.data_ptr(),

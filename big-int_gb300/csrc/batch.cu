@@ -334,6 +334,7 @@ struct bi_plan {
     uint32_t mulw_off[MULW_CLASSES] = {}, n_mulw[MULW_CLASSES] = {};
     uint32_t div_off[DIV_CLASSES] = {}, n_divc[DIV_CLASSES] = {};
     uint32_t max_mul_Lp_full = 0, max_mul_Lp_trunc = 0;
+    uint64_t nflags = 0;                // flag-arena bytes the descriptors were checked against
     size_t mul_smem = 0, div_smem = 0, divc_smem[DIV_CLASSES] = {};
     BatchTune tune = {4, 2, 1, 32};
     cudaGraphExec_t exec = nullptr;
@@ -641,26 +642,67 @@ static void plan_free(bi_plan* p) {
     delete p;
 }
 
+// Descriptor i against the arenas: its op and sizes, and every operand,
+// result and flag it names inside the input arena (in_limbs limbs), the
+// output arena (out_limbs limbs) and the flag arena (nflags bytes; with
+// nflags = 0 the batch writes no flags, so flag offsets are not read).
+static bi_status check_desc(const bi_desc& d, uint64_t i, uint64_t in_limbs, uint64_t out_limbs, uint64_t nflags) {
+    const unsigned long long k = (unsigned long long)i;
+    if (d.m == 0) return set_error(BI_EINVAL, "descriptor %llu: m=0", k);
+    if (d.m > BATCH_MAX_LIMBS) return set_error(BI_EUNSUPPORTED, "descriptor %llu: m=%u", k, d.m);
+    auto inside = [](uint64_t off, uint64_t len, uint64_t size) { return off <= size && len <= size - off; };
+    uint64_t la = d.m, lb = d.m, lr = d.m, lr2 = 0;
+    bool flag = false;
+    switch (d.op) {
+    case BI_OP_ADD: break;
+    case BI_OP_SUB: flag = true; break;
+    case BI_OP_MUL: break;
+    case BI_OP_MULFULL: {
+        const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
+        if (Lp > 2048) return set_error(BI_EUNSUPPORTED, "descriptor %llu: mulfull m=%u", k, d.m);
+        lr = 2ull * d.m;
+        break;
+    }
+    case BI_OP_DIV:
+        if (d.mb == 0 || d.mb > d.m) return set_error(BI_EINVAL, "descriptor %llu: need 1 <= mb <= m", k);
+        lb = d.mb;
+        lr2 = d.mb;
+        flag = true;
+        break;
+    default:
+        return set_error(BI_EINVAL, "descriptor %llu: unknown op %u", k, d.op);
+    }
+    if (!inside(d.a, la, in_limbs) || !inside(d.b, lb, in_limbs))
+        return set_error(BI_EINVAL, "descriptor %llu: operand outside the input arena of %llu limbs", k,
+                         (unsigned long long)in_limbs);
+    if (!inside(d.r, lr, out_limbs) || (lr2 && !inside(d.r2, lr2, out_limbs)))
+        return set_error(BI_EINVAL, "descriptor %llu: result outside the output arena of %llu limbs", k,
+                         (unsigned long long)out_limbs);
+    if (flag && nflags && d.flag >= nflags)
+        return set_error(BI_EINVAL, "descriptor %llu: flag byte %llu outside the flag arena of %llu bytes", k,
+                         (unsigned long long)d.flag, (unsigned long long)nflags);
+    return BI_OK;
+}
+
 }  // namespace bi
 
 extern "C" {
 
-bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t count) {
+bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t count, uint64_t in_limbs,
+                         uint64_t out_limbs, uint64_t nflags) {
     if (!out_plan) return set_error(BI_EINVAL, "out_plan is NULL");
     *out_plan = nullptr;
     if (count && !descs) return set_error(BI_EINVAL, "descs is NULL");
     if (count > 0xffffffffull) return set_error(BI_EINVAL, "too many descriptors");
+    for (uint64_t i = 0; i < count; i++) BI_RETURN_IF(check_desc(descs[i], i, in_limbs, out_limbs, nflags));
     bi_plan* p = new bi_plan();
     cudaGetDevice(&p->device);
     p->count = count;
+    p->nflags = nflags;
     std::vector<uint32_t> addsub, div, mulw[MULW_CLASSES];
     std::vector<std::pair<uint64_t, uint32_t>> mulkeys;   // (bucket key, index)
     for (uint64_t i = 0; i < count; i++) {
         const bi_desc& d = descs[i];
-        if (d.m == 0 || d.m > BATCH_MAX_LIMBS) {
-            plan_free(p);
-            return set_error(d.m == 0 ? BI_EINVAL : BI_EUNSUPPORTED, "descriptor %llu: m=%u", (unsigned long long)i, d.m);
-        }
         switch (d.op) {
         case BI_OP_ADD:
         case BI_OP_SUB:
@@ -670,23 +712,15 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
         case BI_OP_MULFULL: {
             const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
             const uint32_t full = d.op == BI_OP_MULFULL;
-            if (full && Lp > 2048) { plan_free(p); return set_error(BI_EUNSUPPORTED, "descriptor %llu: mulfull m=%u", (unsigned long long)i, d.m); }
             if (full) p->max_mul_Lp_full = std::max(p->max_mul_Lp_full, Lp);
             else p->max_mul_Lp_trunc = std::max(p->max_mul_Lp_trunc, Lp);
             mulkeys.push_back({((uint64_t)full << 40) | ((uint64_t)Lp << 8), (uint32_t)i});
             if (full && d.m <= MULW_MAX_M) mulw[mulw_class(d.m)].push_back((uint32_t)i);
             break;
         }
-        case BI_OP_DIV:
-            if (d.mb == 0 || d.mb > d.m) {
-                plan_free(p);
-                return set_error(BI_EINVAL, "descriptor %llu: need 1 <= mb <= m", (unsigned long long)i);
-            }
+        default:   // BI_OP_DIV (check_desc refused every other op)
             div.push_back((uint32_t)i);
             break;
-        default:
-            plan_free(p);
-            return set_error(BI_EINVAL, "descriptor %llu: unknown op %u", (unsigned long long)i, d.op);
         }
     }
     // largest first: long instances start early, short ones fill the tail
@@ -801,6 +835,7 @@ bi_status bi_plan_execute(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_t
     if (!p) return set_error(BI_EINVAL, "NULL plan");
     if (p->count == 0) return BI_OK;
     if (!in || !out) return set_error(BI_EINVAL, "NULL arena");
+    if (flags && p->nflags == 0) return set_error(BI_EINVAL, "flags given to a plan created with nflags = 0");
     if ((uintptr_t)in % 16 || (uintptr_t)out % 16) return set_error(BI_EINVAL, "arenas must be 16-byte aligned");
     std::lock_guard<std::mutex> lk(p->mu);
     if (!p->exec || p->g_in != in || p->g_out != out || p->g_flags != flags ||
@@ -858,6 +893,7 @@ bi_status bi_plan_autotune(bi_plan* p, const uint64_t* in, uint64_t* out, uint8_
     if (!p) return set_error(BI_EINVAL, "NULL plan");
     if (p->count == 0) return BI_OK;
     if (!in || !out) return set_error(BI_EINVAL, "NULL arena");
+    if (flags && p->nflags == 0) return set_error(BI_EINVAL, "flags given to a plan created with nflags = 0");
     if (reps < 1) reps = 1;
     std::lock_guard<std::mutex> lk(p->mu);
     BatchTune best = p->tune;
@@ -955,25 +991,20 @@ static bi_desc na_descs[NOALLOC_MAX_DESCS];
 static uint32_t na_add[NOALLOC_MAX_DESCS], na_mul[NOALLOC_MAX_DESCS], na_div[NOALLOC_MAX_DESCS];
 static std::pair<uint64_t, uint32_t> na_keys[NOALLOC_MAX_DESCS];
 static MulItem na_items[NOALLOC_MAX_DESCS];
-static std::mutex na_mu;                 // guards the staging arrays and the address cache
-static void* na_dev_ptr[256];            // device address of the scratch array, per device
+static std::mutex na_mu;                 // guards the staging arrays
 
-// Device address of the scratch array on the current device, looked up on
-// the first call for that device (the host symbol is not a device address).
+// Device address of the scratch array on the current device: the host-side
+// name of a __device__ variable is not a device address.  Looked up on every
+// call (cheap next to the call's stream synchronisation), so a context that
+// was torn down and created again (cudaDeviceReset) gets its own address.
 static bi_status noalloc_scratch(void** ptr) {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess || dev < 0 || dev >= 256) return set_error(BI_ECUDA, "no current device");
-    if (!na_dev_ptr[dev]) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || p == nullptr) {
-            cudaGetLastError();
-            return set_error(BI_ECUDA, "scratch address lookup: %s", cudaGetErrorString(e));
-        }
-        na_dev_ptr[dev] = p;
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+        cudaGetLastError();
+        return set_error(BI_ECUDA, "scratch address lookup: %s", cudaGetErrorString(e));
     }
-    *ptr = na_dev_ptr[dev];
+    *ptr = p;
     return BI_OK;
 }
 
@@ -981,8 +1012,9 @@ static bi_status noalloc_scratch(void** ptr) {
 
 extern "C" uint32_t bi_batch_noalloc_max_descs(void) { return NOALLOC_MAX_DESCS; }
 
-extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, const uint64_t* in, uint64_t* out,
-                                          uint8_t* flags, bi_stream stream) {
+extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, const uint64_t* in,
+                                          uint64_t in_limbs, uint64_t* out, uint64_t out_limbs, uint8_t* flags,
+                                          uint64_t nflags, bi_stream stream) {
     if (count == 0) return BI_OK;
     if (!descs) return set_error(BI_EINVAL, "descs is NULL");
     if (count > NOALLOC_MAX_DESCS)
@@ -990,6 +1022,18 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
                          NOALLOC_MAX_DESCS, (unsigned long long)count);
     if (!in || !out) return set_error(BI_EINVAL, "NULL arena");
     if ((uintptr_t)in % 16 || (uintptr_t)out % 16) return set_error(BI_EINVAL, "arenas must be 16-byte aligned");
+    if (flags && nflags == 0) return set_error(BI_EINVAL, "flags given with nflags = 0");
+    for (uint64_t i = 0; i < count; i++) BI_RETURN_IF(check_desc(descs[i], i, in_limbs, out_limbs, nflags));
+    // the call stages its lists from host memory and waits for its stream,
+    // which a stream in capture cannot do: refuse it before anything is enqueued
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t ce = cudaStreamIsCapturing((cudaStream_t)stream, &cs);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        return set_error(BI_ECUDA, "bi_batch_run_noalloc: %s", cudaGetErrorString(ce));
+    }
+    if (cs != cudaStreamCaptureStatusNone)
+        return set_error(BI_EUNSUPPORTED, "bi_batch_run_noalloc: the stream is being captured");
     std::lock_guard<std::mutex> lk(na_mu);
     void* scratch = nullptr;
     BI_RETURN_IF(noalloc_scratch(&scratch));
@@ -1001,22 +1045,16 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
     for (uint64_t i = 0; i < count; i++) {
         const bi_desc& d = descs[i];
         na_descs[i] = d;
-        if (d.m == 0 || d.m > BATCH_MAX_LIMBS)
-            return set_error(d.m == 0 ? BI_EINVAL : BI_EUNSUPPORTED, "descriptor %llu: m=%u", (unsigned long long)i, d.m);
         if (d.op == BI_OP_ADD || d.op == BI_OP_SUB) {
             na_add[na++] = (uint32_t)i;
         } else if (d.op == BI_OP_MUL || d.op == BI_OP_MULFULL) {
             const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
             const uint32_t full = d.op == BI_OP_MULFULL;
-            if (full && Lp > 2048) return set_error(BI_EUNSUPPORTED, "descriptor %llu: mulfull m=%u", (unsigned long long)i, d.m);
             if (full) p.max_mul_Lp_full = std::max(p.max_mul_Lp_full, Lp);
             else p.max_mul_Lp_trunc = std::max(p.max_mul_Lp_trunc, Lp);
             na_keys[nk++] = {((uint64_t)full << 40) | ((uint64_t)Lp << 8), (uint32_t)i};
-        } else if (d.op == BI_OP_DIV) {
-            if (d.mb == 0 || d.mb > d.m) return set_error(BI_EINVAL, "descriptor %llu: need 1 <= mb <= m", (unsigned long long)i);
+        } else {   // BI_OP_DIV (check_desc refused every other op)
             na_div[nd++] = (uint32_t)i;
-        } else {
-            return set_error(BI_EINVAL, "descriptor %llu: unknown op %u", (unsigned long long)i, d.op);
         }
     }
     std::stable_sort(na_add, na_add + na, [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
@@ -1043,6 +1081,7 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
         k = end;
     }
     p.count = count;
+    p.nflags = nflags;
     p.n_addsub = na;
     p.n_mul = nm;
     p.n_items = ni;

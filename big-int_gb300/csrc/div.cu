@@ -230,16 +230,13 @@ static void launch_blk(const T* u, const T* v, T* q, T* r, uint8_t* status, uint
     div_blk_kernel<T, VPL, KB, NW><<<grid, NW == 1 ? DIV_WARP_CTA : 32 * NW, 0, s>>>(u, v, q, r, status, n, mu, mv);
 }
 
-// Long division of divisors of 129..DIV_LONG_MAX_MV limbs, KB quotient limbs
-// at a time (divblock.cuh).
+// Long division of divisors of 1025..DIV_LONG_MAX_MV limbs, KB = 8 quotient
+// limbs at a time (divblock.cuh) on two or four warps.
 template <typename T>
 static void launch_div_blk(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
                            uint64_t n, cudaStream_t s) {
     const uint32_t MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
-    if (MV <= 256) launch_blk<T, 8, 4, 1>(u, v, q, r, status, mu, mv, n, s);
-    else if (MV <= 512) launch_blk<T, 16, 8, 1>(u, v, q, r, status, mu, mv, n, s);
-    else if (MV <= 1024) launch_blk<T, 32, 8, 1>(u, v, q, r, status, mu, mv, n, s);
-    else if (MV <= 2048) launch_blk<T, 32, 8, 2>(u, v, q, r, status, mu, mv, n, s);
+    if (MV <= 2048) launch_blk<T, 32, 8, 2>(u, v, q, r, status, mu, mv, n, s);
     else launch_blk<T, 32, 8, 4>(u, v, q, r, status, mu, mv, n, s);
 }
 
@@ -272,7 +269,7 @@ static bi_status div_entry(const T* u, const T* v, T* q, T* r, uint8_t* status, 
     // DIV_SHINV_MAX_MU64 limbs always take long division
     if (method != DIV_SHINV && g.MV <= (uint32_t)DIV_LONG_MAX_MV &&
         (method == DIV_LONG || g.MU > DIV_SHINV_MAX_MU64 || div_use_long(g.MV, n, num_sms()))) {
-        if (g.MV <= 128) {
+        if (g.MV <= (uint32_t)DIV_WARP_MAX_MV) {
             launch_div_warp(u, v, q, r, status, mu, mv, n, (cudaStream_t)s);
             return check_launch("div warp kernel");
         }

@@ -29,10 +29,16 @@
 //   5. the remainder window moves up KB limbs and KB dividend limbs enter at
 //      the bottom.
 // Against one quotient limb per step (divsmall.cuh), the estimate, the
-// ballots, the shuffles and the window slide are paid once per KB limbs, the
-// multiply-subtract's rows have no ballot between them, and while one warp
-// runs its serial small division another warp's rows keep the integer pipe
-// busy.
+// ballots, the shuffles and the window slide are paid once per KB limbs and
+// the multiply-subtract's rows have no ballot between them.  The library uses
+// it for divisors above 1024 limbs, on two (up to 2048 limbs) or four warps:
+// there the one-limb-per-step kernels run out of registers.  Up to 1024 limbs
+// it divides no faster than they do (GB300, 2m/m: 512/256 limbs 7.1M vs 8.1M
+// div/s, 1024/512 1.7M vs 2.1M, 2048/1024 590K vs 607K) -- per quotient limb
+// the rows still cost about 11.5 instructions a limb product and the one-
+// thread small division about 190 instructions, so the count of instructions
+// changes little, and its 255 registers a thread at 32 limbs a lane leave no
+// room to run products ahead of their carry chains.
 //
 // Layout: lane gl (of NL = 32 NW lanes) holds window and divisor positions
 // gl VPL .. gl VPL + VPL - 1 (MX = NL VPL positions); the top lane (gl =
@@ -397,5 +403,6 @@ __device__ __forceinline__ uint8_t div_blk(uint32_t MU, uint32_t MV, LoadU load_
     if constexpr (NW > 1) __syncthreads();   // the shared area is the next division's
     return 0;
 }
+
 
 }  // namespace bi

@@ -317,10 +317,17 @@ typedef struct bi_desc {
 typedef struct bi_plan bi_plan;
 
 /* Build a plan from host descriptors (m <= 2048; mulfull m <= 2048).      */
-/* Allocates device work lists; the plan is bound to the current device.   */
-bi_status bi_plan_create(bi_plan** plan, const bi_desc* descs, uint64_t count);
-/* Run the plan: in/out are device arenas (16-byte aligned), flags may be   */
-/* NULL.  The first call (and any call with other arenas or tuning)        */
+/* in_limbs, out_limbs: limbs of the input and output arenas the plan     */
+/* will run on; nflags: bytes of its flag arena (0: no flag arena, and    */
+/* bi_plan_execute then takes flags = NULL).  Every operand, result and    */
+/* flag a descriptor names must lie inside its arena, else BI_EINVAL       */
+/* before anything is allocated.  Allocates device work lists; the plan is */
+/* bound to the current device.                                            */
+bi_status bi_plan_create(bi_plan** plan, const bi_desc* descs, uint64_t count,
+                         uint64_t in_limbs, uint64_t out_limbs, uint64_t nflags);
+/* Run the plan: in/out are device arenas (16-byte aligned) of at least    */
+/* the sizes the plan was built for, flags may be NULL.  The first call    */
+/* (and any call with other arenas or tuning)                              */
 /* captures the CUDA graph; later calls replay it on `stream`.  Calls on    */
 /* one plan are serialised; its launches must not overlap on the device.   */
 bi_status bi_plan_execute(bi_plan* plan, const uint64_t* in, uint64_t* out,
@@ -358,17 +365,21 @@ bi_status bi_plan_destroy(bi_plan* plan);
 /* fixed device array owned by the library (about 344 KB, held on every    */
 /* GPU that loads the library until the process exits).  At most          */
 /* bi_batch_noalloc_max_descs() descriptors (4096) per call; larger counts */
-/* are rejected with BI_EINVAL.  Same descriptors, arenas and results as   */
-/* bi_plan_execute; descs is host memory.  The first call on each device   */
-/* looks up the array's device address, so make it before any stream      */
-/* capture.  Every call shares the one array: calls that overlap on the    */
-/* GPU race, so issue them one after another (the call returns when its    */
-/* work on `stream` has finished).                                         */
+/* are rejected with BI_EINVAL, and so is any descriptor whose operands,   */
+/* results or flag leave the arenas (in_limbs, out_limbs limbs; nflags     */
+/* bytes, 0 when flags is NULL).  Same descriptors, arenas and results as  */
+/* bi_plan_execute; descs is host memory.  Each call looks up the array's  */
+/* device address on the current device, stages its lists from host       */
+/* memory and returns when its work on `stream` has finished; a stream     */
+/* that is being captured is refused with BI_EUNSUPPORTED before anything */
+/* is enqueued.  Every call shares the one array: calls that overlap on    */
+/* the GPU race, so issue them one after another.                          */
 /* ---------------------------------------------------------------------- */
 uint32_t bi_batch_noalloc_max_descs(void);
 bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count,
-                               const uint64_t* in, uint64_t* out, uint8_t* flags,
-                               bi_stream stream);
+                               const uint64_t* in, uint64_t in_limbs,
+                               uint64_t* out, uint64_t out_limbs,
+                               uint8_t* flags, uint64_t nflags, bi_stream stream);
 
 /* ---------------------------------------------------------------------- */
 /* Serving loop: requests of any operation and size, submitted one at a    */

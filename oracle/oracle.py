@@ -24,9 +24,20 @@ _lib = None
 _ref = None
 
 
+def reference_checkout():
+    """The reference checkout whose prototypes/div.c is compiled beside the
+    oracle: $BIGINT_REF, else a `reference` directory beside the
+    repository; None when neither exists."""
+    for cand in (os.environ.get("BIGINT_REF"), os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")):
+        if cand and os.path.isdir(cand):
+            return cand
+    return None
+
+
 def build(quiet: bool = True) -> None:
     """Compile the oracle (and the reference's div.c where present)."""
-    out = subprocess.run(["make", "-C", HERE, "all"], capture_output=True, text=True)
+    ref = reference_checkout()
+    out = subprocess.run(["make", "-C", HERE, "all"] + ([f"REF={ref}"] if ref else []), capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

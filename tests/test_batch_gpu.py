@@ -16,7 +16,7 @@ def _groups(d):
     return keys
 
 
-def check_batch(B, oracle, d, arena, out, flags):
+def check_batch(B, oracle, d, arena, out, flags, nthreads=1):
     """Compare every instance of the batch with the oracle, grouped by shape."""
     for (op, m, mb), idx in _groups(d).items():
         idx = np.array(idx)
@@ -32,14 +32,14 @@ def check_batch(B, oracle, d, arena, out, flags):
             assert (flags[d["flag"][idx]] == s).all(), ("sub sign", m)
         elif op == B.OP_MULFULL:
             got = np.stack([out[d["r"][i]: d["r"][i] + 2 * m] for i in idx])
-            assert (got == oracle.mulfull(a, b)).all(), ("mulfull", m)
+            assert (got == oracle.mulfull(a, b, nthreads=nthreads)).all(), ("mulfull", m)
         elif op == B.OP_MUL:
             got = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
-            assert (got == oracle.mul(a, b)).all(), ("mul", m)
+            assert (got == oracle.mul(a, b, nthreads=nthreads)).all(), ("mul", m)
         else:
             q = np.stack([out[d["r"][i]: d["r"][i] + m] for i in idx])
             r = np.stack([out[d["r2"][i]: d["r2"][i] + mb] for i in idx])
-            qo, ro, so = oracle.div(a, b)
+            qo, ro, so = oracle.div(a, b, nthreads=nthreads)
             assert (q == qo).all() and (r == ro).all(), ("div", m, mb)
             assert (flags[d["flag"][idx]] == so).all()
 
@@ -50,7 +50,7 @@ def _run(B, d, arena, out_limbs, nflags, tune=None, autotune=False):
     din = B.to_device(arena)
     dout = torch.zeros(max(1, out_limbs), dtype=torch.int64, device="cuda")
     dfl = torch.zeros(max(1, nflags), dtype=torch.uint8, device="cuda")
-    plan = B.Plan(d)
+    plan = B.Plan(d, len(arena), dout.numel(), dfl.numel())
     if tune:
         plan.set_tuning(*tune)
     if autotune:
@@ -184,17 +184,25 @@ def test_batch_matches_per_size_kernels(bigint):
     torch.cuda.synchronize()
 
 
-def test_full_size_batch_matches_per_size_kernels(bigint):
+def test_full_size_batch_matches_per_size_kernels(bigint, oracle):
     """The benchmark's batch itself (100000 instances, 256..65536 bits, the
     mix and seed of the uneven-batch workload): every instance equals the
-    plain per-size kernels' result, and a sample of the divisions satisfies
-    u = q v + r with r < v in Python integers."""
+    plain per-size kernels' result; 3000 instances sampled across every op
+    and size equal the oracle's (the per-size kernels and the batch share
+    their multiply and division cores, so this catches a defect common to
+    both); and a sample of the divisions satisfies u = q v + r with r < v in
+    Python integers."""
+    import os
+
     import torch
 
     B = bigint
     d, arena, out_limbs, nflags = B.workloads.uneven_batch()
     plan, din, dout, dfl = _run(B, d, arena, out_limbs, nflags)
     out = B.to_host(dout, np.uint64)
+    flags = dfl.cpu().numpy()
+    sample = np.sort(np.random.default_rng(7).choice(len(d), size=3000, replace=False))
+    check_batch(B, oracle, d[sample], arena, out, flags, nthreads=os.cpu_count() or 1)
 
     def rows(src, off, idx, width):
         return src[d[off][idx].astype(np.int64)[:, None] + np.arange(width)]
@@ -231,8 +239,8 @@ def test_invalid_descriptors_rejected(bigint):
     for bad in [dict(op=0, m=0, mb=0), dict(op=9, m=4, mb=4), dict(op=4, m=4, mb=5), dict(op=0, m=5000, mb=5000)]:
         d[0]["op"], d[0]["m"], d[0]["mb"] = bad["op"], bad["m"], bad["mb"]
         with pytest.raises(B.BigIntError):
-            B.Plan(d)
-    empty = B.Plan(np.zeros(0, dtype=B.DESC_DTYPE))
+            B.Plan(d, 1 << 20, 1 << 20, 16)
+    empty = B.Plan(np.zeros(0, dtype=B.DESC_DTYPE), 0, 0)
     assert empty.stats()["addsub"] == 0
     empty.close()
 
@@ -269,7 +277,7 @@ def test_small_full_products_at_either_word_width(bigint, oracle, bits):
     din = B.to_device(arena)
     dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
     dfl = torch.zeros(1, dtype=torch.uint8, device="cuda")
-    plan = B.Plan(d)
+    plan = B.Plan(d, len(arena), out_limbs, 1)
     plan.set_mul_word_bits(bits)
     assert plan.tuning()["mul_small_word_bits"] == bits
     plan.execute(din, dout, dfl)
@@ -288,7 +296,7 @@ def test_autotune_picks_a_word_width(bigint, oracle):
     din = B.to_device(arena)
     dout = torch.zeros(out_limbs, dtype=torch.int64, device="cuda")
     dfl = torch.zeros(1, dtype=torch.uint8, device="cuda")
-    plan = B.Plan(d)
+    plan = B.Plan(d, len(arena), out_limbs, 1)
     t = plan.autotune(din, dout, dfl, reps=1)
     assert t["mul_small_word_bits"] in (32, 64) and t == plan.tuning()
     dout.zero_()

@@ -6,6 +6,7 @@ import glob
 import os
 import re
 
+import numpy as np
 import pytest
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -134,3 +135,46 @@ def test_plan_tuning_arguments_checked_on_host(L):
     assert L.bi_plan_get_tuning(None, ctypes.cast(t, ctypes.c_void_p)) == 1
     assert L.bi_plan_set_tuning(None, 4, 2, 1) == 1
     assert L.bi_plan_autotune(None, None, None, None, 1, None) == 1
+
+
+def _desc(B, op, m, mb, a, b, r, r2=0, flag=0):
+    d = np.zeros(1, dtype=B.DESC_DTYPE)
+    d[0]["op"], d[0]["m"], d[0]["mb"] = op, m, mb
+    d[0]["a"], d[0]["b"], d[0]["r"], d[0]["r2"], d[0]["flag"] = a, b, r, r2, flag
+    return d
+
+
+def test_batch_descriptors_checked_against_arenas_on_host(L):
+    """Every operand, result and flag a batch descriptor names must lie inside
+    its arena: out-of-range offsets for each op are refused with BI_EINVAL by
+    bi_plan_create and bi_batch_run_noalloc before any device work (the
+    arena pointers below are never dereferenced)."""
+    import bigint_gb300 as B
+
+    IN, OUT, NF = 1000, 1000, 10
+    cases = []
+    for op in (B.OP_ADD, B.OP_SUB, B.OP_MUL, B.OP_MULFULL, B.OP_DIV):
+        m, mb = 40, (20 if op == B.OP_DIV else 40)
+        lr = 2 * m if op == B.OP_MULFULL else m
+        cases += [
+            _desc(B, op, m, mb, IN - m + 1, 0, 0, 500, 0),           # a runs past the input arena
+            _desc(B, op, m, mb, 0, IN - mb + 1, 0, 500, 0),          # b runs past it
+            _desc(B, op, m, mb, 0, 100, OUT - lr + 1, 0, 0),         # r runs past the output arena
+            _desc(B, op, m, mb, 0, 100, 2 ** 64 - 8, 500, 0),        # an offset that wraps
+        ]
+        if op == B.OP_DIV:
+            cases.append(_desc(B, op, m, mb, 0, 100, 0, OUT - mb + 1, 0))   # r2 runs past it
+        if op in (B.OP_SUB, B.OP_DIV):
+            cases.append(_desc(B, op, m, mb, 0, 100, 0, 500, NF))          # flag past the flag arena
+    fake = ctypes.c_void_p(4096)                                      # 16-byte aligned, never read
+    for d in cases:
+        h = ctypes.c_void_p()
+        st = L.bi_plan_create(ctypes.byref(h), d.ctypes.data_as(ctypes.c_void_p), 1, IN, OUT, NF)
+        assert st == 1 and not h.value, (d, L.bi_last_error())
+        assert b"outside" in L.bi_last_error()
+        st = L.bi_batch_run_noalloc(d.ctypes.data_as(ctypes.c_void_p), 1, fake, IN, fake, OUT, fake, NF, None)
+        assert st == 1 and b"outside" in L.bi_last_error(), (d, L.bi_last_error())
+    # flags without a flag arena
+    d = _desc(B, B.OP_ADD, 4, 4, 0, 4, 0)
+    st = L.bi_batch_run_noalloc(d.ctypes.data_as(ctypes.c_void_p), 1, fake, IN, fake, OUT, fake, 0, None)
+    assert st == 1 and b"nflags" in L.bi_last_error()

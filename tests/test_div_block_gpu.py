@@ -1,10 +1,12 @@
-"""GPU parity of long division KB quotient limbs at a time (divblock.cuh),
-the method for divisors of 129..4096 64-bit limbs, against the oracle: every
-warp shape and its boundaries, ragged u32 sizes, divisors shorter than their
-rows, dividends that pad the first quotient block, inputs whose block
-estimate is capped at B^KB - 1 or one too large (the add-back), zero
-divisors and dividends smaller than the divisor, and the 8192 / 4096-limb
-division of the largest full product."""
+"""GPU parity of long division against the oracle across the divisor sizes
+where the kernels change: the one-limb-per-step warp and lane-group kernels
+up to 1024 64-bit limbs, and above that long division KB quotient limbs at a
+time on two or four warps (divblock.cuh) up to 4096-limb divisors and
+8192-limb dividends -- ragged u32 sizes, divisors shorter than their rows,
+dividends that pad the first quotient block, inputs whose block estimate is
+capped at B^KB - 1 or one too large (the add-back), zero divisors and
+dividends smaller than the divisor, and the 8192 / 4096-limb division of the
+largest full product."""
 import random
 
 import numpy as np
@@ -32,8 +34,8 @@ def _run(B, oracle, u, v, method="long"):
     assert bad.size == 0, f"{bad.size} mismatching rows, first {bad[:5]}"
 
 
-# divisor sizes on both sides of each shape: 8 limbs a lane on one warp up
-# to 256, 16 up to 512, 32 up to 1024, then two and four warps of 32
+# divisor sizes on both sides of each kernel shape: lane groups and warps up
+# to 1024 limbs, then the blocked kernel on two warps up to 2048 and four up to 4096
 @pytest.mark.parametrize("mv", [129, 200, 256, 257, 400, 512, 513, 777, 1024, 1025, 1500, 2048, 2049, 4096])
 def test_shapes_dividend_twice_divisor(bigint, oracle, mv):
     n = 4 if mv > 1024 else 8
@@ -48,22 +50,21 @@ def test_shapes_dividend_twice_divisor(bigint, oracle, mv):
     _run(bigint, oracle, u, v)
 
 
-@pytest.mark.parametrize("mu", [130, 131, 136, 137, 138, 150, 300, 1000, 3000])
+@pytest.mark.parametrize("mu", [1026, 1027, 1029, 1032, 1033, 1034, 1040, 1100, 2500])
 def test_first_block_padding(bigint, oracle, mu):
-    """129-limb divisors with dividends whose quotient length is every residue
-    modulo the block size (4 and 8 limbs), from one limb up."""
-    mv = 129
-    n = 6
+    """1025-limb divisors with dividends whose quotient length takes every
+    residue modulo the 8-limb block, from one quotient limb up; and a
+    divisor two limbs shorter than its 1025-limb row."""
+    mv = 1025
+    n = 4
     u = uniform_limbs(5300 + mu, n, mu)
     v = uniform_limbs(5400 + mu, n, mv)
     v[:, -1] |= 1
     u[1, -1] = 0                                  # the top dividend limb zero
     u[2] = M64
+    v[3, -2:] = 0
+    v[3, -3] |= 1
     _run(bigint, oracle, u, v)
-    v8 = uniform_limbs(5500 + mu, n, 300)
-    v8[:, -1] |= 1
-    if mu >= 300:
-        _run(bigint, oracle, uniform_limbs(5600 + mu, n, mu), v8)
 
 
 @pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
@@ -168,11 +169,11 @@ def _pyint_rows(a):
 
 @pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
 def test_many_instances(bigint, oracle, dtype):
-    """Enough 512/256 and 2048/1024 divisions to fill every warp several
-    times: the first 16 rows against the oracle, every row exactly in Python
-    integers (u = q v + r, r < v)."""
+    """Enough 512/256, 2048/1024 and 3000/1500 divisions to fill every warp
+    several times: the first 16 rows against the oracle, every row exactly
+    in Python integers (u = q v + r, r < v)."""
     B = bigint
-    for mv, n in [(256, 3000), (1024, 1400)]:
+    for mv, n in [(256, 3000), (1024, 1400), (1500, 700)]:
         w = 2 if dtype == np.uint32 else 1
         u = uniform_limbs(6300 + mv, n, 2 * mv * w, dtype)
         v = uniform_limbs(6400 + mv, n, mv * w, dtype)
