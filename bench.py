@@ -614,6 +614,20 @@ def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100
     def short(rep):
         return {k: (round(rep[k], 2) if isinstance(rep[k], float) else rep[k]) for k in keep}
 
+    def per_class(d, lat_ns):
+        """p50 / p99 latency (us) and count per (op, operand limbs) class."""
+        lat = lat_ns.astype(np.float64) / 1e3
+        names = {B.OP_ADD: "add", B.OP_SUB: "sub", B.OP_MULFULL: "mulfull", B.OP_DIV: "div"}
+        res = {}
+        for op, name in names.items():
+            for lo, hi in ((1, 64), (65, 256), (257, 512)):
+                sel = (d["op"] == op) & (d["m"] >= lo) & (d["m"] <= hi)
+                if sel.sum() >= 20:
+                    x = lat[sel]
+                    res[f"{name}_m{lo}-{hi}"] = [int(sel.sum()), round(float(np.percentile(x, 50)), 1),
+                                                 round(float(np.percentile(x, 99)), 1)]
+        return res
+
     out = {}
     beyond = {}
     with B.Server(pool, arena) as srv:
@@ -621,8 +635,8 @@ def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100
         srv.replay(warm[0], warm[1])
         for r in rates:
             d, arr, _ = streams_of[r]
-            _, _, rep = srv.replay(d, arr)
-            out[str(r)] = {"loop": short(rep)}
+            lat, _, rep = srv.replay(d, arr)
+            out[str(r)] = {"loop": short(rep), "loop_per_class_n_p50_p99_us": per_class(d, lat)}
         # past the offered loads: where the loop saturates
         for r in saturation_rates:
             d, arr, _ = serve_stream(max_requests, r, seed=1005, pool_limbs=pool_limbs)
@@ -632,8 +646,9 @@ def measure_serving(B, rates=None, seconds: float = 0.2, max_requests: int = 100
     B.replay_plain(pool, arena, warm[0], warm[1], streams=streams)
     for r in rates:
         d, arr, _ = streams_of[r]
-        _, _, rep = B.replay_plain(pool, arena, d, arr, streams=streams)
+        lat, _, rep = B.replay_plain(pool, arena, d, arr, streams=streams)
         out[str(r)]["per_request_launch"] = short(rep)
+        out[str(r)]["launch_per_class_n_p50_p99_us"] = per_class(d, lat)
         lo, pl = out[str(r)]["loop"], out[str(r)]["per_request_launch"]
         out[str(r)]["p99_ratio_launch_over_loop"] = round(pl["p99_us"] / lo["p99_us"], 2) if lo["p99_us"] else None
     del pool, arena

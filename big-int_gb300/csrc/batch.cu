@@ -31,6 +31,7 @@
 #include <mutex>
 #include <vector>
 
+#include "divblock.cuh"
 #include "divcore.cuh"
 #include "divsmall.cuh"
 #include "mulcore.cuh"
@@ -39,7 +40,10 @@
 
 namespace bi {
 
-constexpr uint32_t BATCH_MAX_LIMBS = 2048;   // per operand (64-bit limbs)
+constexpr uint32_t BATCH_MAX_LIMBS = 2048;   // per operand (64-bit limbs), add/sub and multiplies
+constexpr uint32_t BATCH_DIV_MAX_M = 8192;   // a division's dividend limbs
+constexpr uint32_t BATCH_DIV_MAX_MB = DIV_LONG_MAX_MV;   // and divisor limbs
+constexpr uint32_t BATCH_SHINV_MAX_M = 2048; // the shifted inverse keeps its operands in shared memory
 
 struct MulItem {
     uint32_t first;   // index into the mul list
@@ -177,11 +181,14 @@ batch_mulwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restri
 }
 
 // division classes by divisor limbs: long division on threads (divisors up
-// to 4, 8, 16 limbs), on warps (up to 32, 64, ..., 1024 limbs), the shifted
-// inverse on 512-thread CTAs above
+// to 4, 8, 16 limbs), on warps (up to 32, 64, ..., 1024 limbs), block long
+// division on two warps (up to 2048 limbs) and four warps (up to 4096); the
+// shifted inverse on 512-thread CTAs is the class that a size class above
+// 128 limbs with few divisions runs as
 constexpr int DIV_THREAD_CLASSES = 3, DIV_WARP_CLASSES = 6;
 constexpr int DIV_CTA_CLASS = DIV_THREAD_CLASSES + DIV_WARP_CLASSES;
-constexpr int DIV_CLASSES = DIV_CTA_CLASS + 1;
+constexpr int DIV_BLK2_CLASS = DIV_CTA_CLASS + 1, DIV_BLK4_CLASS = DIV_CTA_CLASS + 2;
+constexpr int DIV_CLASSES = DIV_CTA_CLASS + 3;
 constexpr int DIV_CTA_THREADS = 512;
 // add/sub, multiply, one per division class, one per warp-multiply class
 constexpr int PLAN_KERNELS = 2 + DIV_CLASSES + MULW_CLASSES;
@@ -191,7 +198,7 @@ static inline int div_class(uint32_t mv) {
     if (mv <= 4) return 0;
     if (mv <= 8) return 1;
     if (mv <= 16) return 2;
-    if (mv > (uint32_t)DIV_WARP_MAX_MV) return DIV_CTA_CLASS;
+    if (mv > (uint32_t)DIV_WARP_MAX_MV) return mv <= 2048 ? DIV_BLK2_CLASS : DIV_BLK4_CLASS;
     int c = DIV_THREAD_CLASSES;
     for (uint32_t cap = 32; cap < mv; cap *= 2) c++;
     return c;
@@ -319,6 +326,32 @@ static bi_status dev_upload(T** dst, const std::vector<T>& v, cudaStream_t s) {
 
 using namespace bi;
 
+// Divisions by 1025..4096-limb divisors: block long division (divblock.cuh)
+// on the CTA's NW warps, one division at a time.
+template <int NW>
+__global__ void __launch_bounds__(32 * NW)
+batch_divblk_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                    uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    __shared__ DivBlkShared<8, NW> sh;
+    __shared__ uint32_t s_idx;
+    for (;;) {
+        if (threadIdx.x == 0) s_idx = atomicAdd(counter, 1u);
+        __syncthreads();
+        const uint32_t idx = s_idx;
+        __syncthreads();
+        if (idx >= count) break;
+        const bi_desc d = descs[list[idx]];
+        const uint64_t* u = in + d.a;
+        const uint64_t* v = in + d.b;
+        uint64_t* q = out + d.r;
+        uint64_t* r = out + d.r2;
+        const uint8_t st = div_blk<32, 8, NW>(
+            d.m, d.mb, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
+            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; }, &sh);
+        if (flags && threadIdx.x == 0) flags[d.flag] = st;
+    }
+}
+
 struct bi_plan {
     int device = 0;
     uint64_t count = 0;
@@ -375,10 +408,15 @@ static size_t mul_smem_for(const bi_plan* p, int ipc_div) {
 // class that size class c runs as.
 static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n, int sms, int* map) {
     uint64_t cnt[DIV_CLASSES] = {};
-    for (uint32_t k = 0; k < n; k++) cnt[div_class(descs[div[k]].mb)]++;
+    uint32_t max_m[DIV_CLASSES] = {};
+    for (uint32_t k = 0; k < n; k++) {
+        const int c = div_class(descs[div[k]].mb);
+        cnt[c]++;
+        max_m[c] = std::max(max_m[c], descs[div[k]].m);
+    }
     for (int c = 0; c < DIV_CLASSES; c++) {
         map[c] = c;
-        if (c >= DIV_THREAD_CLASSES && c < DIV_CTA_CLASS) {
+        if (c >= DIV_THREAD_CLASSES && c < DIV_CTA_CLASS && max_m[c] <= BATCH_SHINV_MAX_M) {
             const uint32_t max_mv = 32u << (c - DIV_THREAD_CLASSES);   // the class's largest divisor
             if (max_mv > 128) {
                 const uint64_t per_sm = max_mv <= 256 ? 2 : max_mv <= 512 ? 3 : 6;
@@ -430,8 +468,11 @@ static bi_status grid_for(const void* k, int threads, size_t smem, uint64_t work
 
 // The kernel of division class c (host-side function pointer) and its CTA width.
 static const void* div_class_kernel(int c, int* threads) {
-    *threads = c < DIV_THREAD_CLASSES ? DIV_THREAD_CTA : c < DIV_CTA_CLASS ? DIV_WARP_CTA : DIV_CTA_THREADS;
+    *threads = c < DIV_THREAD_CLASSES ? DIV_THREAD_CTA : c < DIV_CTA_CLASS ? DIV_WARP_CTA
+               : c == DIV_BLK2_CLASS ? 64 : c == DIV_BLK4_CLASS ? 128 : DIV_CTA_THREADS;
     switch (c) {
+    case DIV_BLK2_CLASS: return (const void*)batch_divblk_kernel<2>;
+    case DIV_BLK4_CLASS: return (const void*)batch_divblk_kernel<4>;
     case 0: return (const void*)batch_divthread_kernel<4>;
     case 1: return (const void*)batch_divthread_kernel<8>;
     case 2: return (const void*)batch_divthread_kernel<16>;
@@ -573,6 +614,8 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
             case 6: batch_divwarp_kernel<8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 7: batch_divwarp_kernel<16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 8: batch_divwarp_kernel<32><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case DIV_BLK2_CLASS: batch_divblk_kernel<2><<<grid, 64, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case DIV_BLK4_CLASS: batch_divblk_kernel<4><<<grid, 128, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             default:
                 batch_div_kernel<DIV_CTA_THREADS><<<grid, DIV_CTA_THREADS, L.smem[2 + c], st>>>(p->d_descs, list, n, ctr,
                                                                                              in, out, flags);
@@ -649,7 +692,8 @@ static void plan_free(bi_plan* p) {
 static bi_status check_desc(const bi_desc& d, uint64_t i, uint64_t in_limbs, uint64_t out_limbs, uint64_t nflags) {
     const unsigned long long k = (unsigned long long)i;
     if (d.m == 0) return set_error(BI_EINVAL, "descriptor %llu: m=0", k);
-    if (d.m > BATCH_MAX_LIMBS) return set_error(BI_EUNSUPPORTED, "descriptor %llu: m=%u", k, d.m);
+    if (d.op == BI_OP_DIV ? (d.m > BATCH_DIV_MAX_M || d.mb > BATCH_DIV_MAX_MB) : d.m > BATCH_MAX_LIMBS)
+        return set_error(BI_EUNSUPPORTED, "descriptor %llu: m=%u mb=%u above the batch's limits", k, d.m, d.mb);
     auto inside = [](uint64_t off, uint64_t len, uint64_t size) { return off <= size && len <= size - off; };
     uint64_t la = d.m, lb = d.m, lr = d.m, lr2 = 0;
     bool flag = false;

@@ -316,7 +316,8 @@ typedef struct bi_desc {
 
 typedef struct bi_plan bi_plan;
 
-/* Build a plan from host descriptors (m <= 2048; mulfull m <= 2048).      */
+/* Build a plan from host descriptors (m <= 2048 for add, sub and the     */
+/* multiplies; a division's dividend m <= 8192 and divisor mb <= 4096).    */
 /* in_limbs, out_limbs: limbs of the input and output arenas the plan     */
 /* will run on; nflags: bytes of its flag arena (0: no flag arena, and    */
 /* bi_plan_execute then takes flags = NULL).  Every operand, result and    */

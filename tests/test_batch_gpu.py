@@ -304,3 +304,51 @@ def test_autotune_picks_a_word_width(bigint, oracle):
     torch.cuda.synchronize()
     check_batch(B, oracle, d, arena, B.to_host(dout, np.uint64), dfl.cpu().numpy())
     plan.close()
+
+
+def test_large_divisions_in_a_batch(bigint, oracle):
+    """Divisions beyond the one-limb-per-step kernels' reach inside a mixed
+    batch: divisors of 1025..4096 limbs (block long division on two and four
+    warps) with dividends up to 8192 limbs, and a few 500-1000-limb divisors
+    of dividends longer than the shifted inverse takes (they stay on long
+    division), beside additions and products."""
+    B = bigint
+    rng = np.random.default_rng(77)
+    shapes = [(2100, 1025), (4000, 2048), (4100, 2049), (8192, 4096), (3000, 1500), (3000, 600), (2500, 900)]
+    ops = [(B.OP_DIV, m, mb) for m, mb in shapes] + [(B.OP_ADD, 300, 300), (B.OP_MULFULL, 200, 200),
+                                                     (B.OP_SUB, 64, 64), (B.OP_DIV, 40, 20)]
+    d = np.zeros(len(ops), dtype=B.DESC_DTYPE)
+    pos = out = 0
+    for i, (op, m, mb) in enumerate(ops):
+        d[i]["op"], d[i]["m"], d[i]["mb"] = op, m, mb
+        d[i]["a"], d[i]["b"] = pos, pos + m
+        pos += m + mb
+        d[i]["r"] = out
+        out += 2 * m if op == B.OP_MULFULL else m
+        if op == B.OP_DIV:
+            d[i]["r2"] = out
+            out += mb
+        d[i]["flag"] = i
+    arena = rng.integers(0, 2**64, size=pos, dtype=np.uint64)
+    for i, (op, m, mb) in enumerate(ops):
+        if op == B.OP_DIV:
+            arena[d[i]["b"] + mb - 1] |= np.uint64(1 << 63)
+    arena[d[1]["a"]: d[1]["a"] + 4000] = np.uint64(0xFFFFFFFFFFFFFFFF)   # an all-ones dividend
+    plan, din, dout, dfl = _run(B, d, arena, out, len(ops))
+    import os
+    check_batch(B, oracle, d, arena, B.to_host(dout, np.uint64), dfl.cpu().numpy(), nthreads=os.cpu_count() or 1)
+    plan.close()
+
+
+def test_batch_size_limits_rejected(bigint):
+    """Sizes past the batch's limits are refused when the plan is built."""
+    B = bigint
+    for op, m, mb in [(B.OP_ADD, 2049, 2049), (B.OP_MULFULL, 2049, 2049), (B.OP_DIV, 8193, 100),
+                      (B.OP_DIV, 8192, 4097)]:
+        d = np.zeros(1, dtype=B.DESC_DTYPE)
+        d[0]["op"], d[0]["m"], d[0]["mb"] = op, m, mb
+        d[0]["b"] = m
+        with pytest.raises(B.BigIntError) as ei:
+            B.Plan(d, 1 << 20, 1 << 20, 16)
+        assert ei.value.status == 6             # BI_EUNSUPPORTED
+
