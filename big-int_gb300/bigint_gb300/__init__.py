@@ -441,7 +441,7 @@ def probe_intpipe(stream=None) -> dict:
 
 OP_ADD, OP_SUB, OP_MUL, OP_MULFULL, OP_DIV = 0, 1, 2, 3, 4
 
-DESC_DTYPE = np.dtype([("op", "<u4"), ("m", "<u4"), ("mb", "<u4"), ("reserved", "<u4"),
+DESC_DTYPE = np.dtype([("op", "<u4"), ("m", "<u4"), ("mb", "<u4"), ("width", "<u4"),
                        ("a", "<u8"), ("b", "<u8"), ("r", "<u8"), ("r2", "<u8"), ("flag", "<u8")])
 
 

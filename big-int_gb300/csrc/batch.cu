@@ -45,6 +45,32 @@ constexpr uint32_t BATCH_DIV_MAX_M = 8192;   // a division's dividend limbs
 constexpr uint32_t BATCH_DIV_MAX_MB = DIV_LONG_MAX_MV;   // and divisor limbs
 constexpr uint32_t BATCH_SHINV_MAX_M = 2048; // the shifted inverse keeps its operands in shared memory
 
+// A descriptor's elements: 64-bit limbs (width 0 or 64) or 32-bit words
+// (width 32: m, mb and the offsets count words of the arenas).  The kernels
+// work on 64-bit limbs either way: a word instance is read as the limbs of
+// its zero-extended value and written back word by word.
+__host__ __device__ inline bool desc_w32(const bi_desc& d) { return d.width == 32; }
+__host__ __device__ inline uint32_t m64(const bi_desc& d) { return desc_w32(d) ? (d.m + 1) / 2 : d.m; }
+__host__ __device__ inline uint32_t mb64(const bi_desc& d) { return desc_w32(d) ? (d.mb + 1) / 2 : d.mb; }
+// 64-bit limb i of the n-element operand at element offset off of an arena
+__device__ __forceinline__ uint64_t ld64(const uint64_t* arena, uint64_t off, uint32_t n, bool w32, uint32_t i) {
+    if (!w32) return i < n ? arena[off + i] : 0;
+    const uint32_t* p = reinterpret_cast<const uint32_t*>(arena) + off;
+    uint64_t x = 2 * i < n ? p[2 * i] : 0u;
+    if (2 * i + 1 < n) x |= (uint64_t)p[2 * i + 1] << 32;
+    return x;
+}
+// limb i of an n-element result: the elements of it that lie below n
+__device__ __forceinline__ void st64(uint64_t* arena, uint64_t off, uint32_t n, bool w32, uint32_t i, uint64_t v) {
+    if (!w32) {
+        if (i < n) arena[off + i] = v;
+        return;
+    }
+    uint32_t* p = reinterpret_cast<uint32_t*>(arena) + off;
+    if (2 * i < n) p[2 * i] = (uint32_t)v;
+    if (2 * i + 1 < n) p[2 * i + 1] = (uint32_t)(v >> 32);
+}
+
 struct MulItem {
     uint32_t first;   // index into the mul list
     uint32_t count;   // instances in this item
@@ -83,11 +109,24 @@ batch_addsub_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restric
         const bi_desc d = descs[list[idx]];
         const bool sub = d.op == BI_OP_SUB;
         uint8_t* sg = (sub && flags) ? flags + d.flag : nullptr;
-        // 16-byte accesses need even limb offsets (the arenas are 16-byte aligned)
-        if (VEC == 2 && ((d.a | d.b | d.r) & 1ull) == 0)
+        if (desc_w32(d)) {
+            if (((d.a | d.b | d.r | d.m) & 1ull) == 0) {   // whole 64-bit limbs: the same bytes as m / 2 limbs
+                const bi_desc e = {d.op, d.m / 2, d.m / 2, 0, d.a / 2, d.b / 2, d.r / 2, 0, d.flag};
+                if (VEC == 2 && ((e.a | e.b | e.r) & 1ull) == 0)
+                    warp_addsub<VEC, R>(in + e.a, in + e.b, out + e.r, sg, e.m, sub);
+                else
+                    warp_addsub<1, R>(in + e.a, in + e.b, out + e.r, sg, e.m, sub);
+            } else {
+                const uint32_t* in32 = reinterpret_cast<const uint32_t*>(in);
+                warp_addsub<1, R, uint32_t>(in32 + d.a, in32 + d.b, reinterpret_cast<uint32_t*>(out) + d.r, sg, d.m,
+                                            sub);
+            }
+        } else if (VEC == 2 && ((d.a | d.b | d.r) & 1ull) == 0) {
+            // 16-byte accesses need even limb offsets (the arenas are 16-byte aligned)
             warp_addsub<VEC, R>(in + d.a, in + d.b, out + d.r, sg, d.m, sub);
-        else
+        } else {
             warp_addsub<1, R>(in + d.a, in + d.b, out + d.r, sg, d.m, sub);
+        }
     }
 }
 
@@ -103,7 +142,8 @@ batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
     extern __shared__ __align__(16) uint64_t smem[];
     __shared__ uint32_t s_item;
     __shared__ uint64_t s_a[BATCH_CTA], s_b[BATCH_CTA], s_r[BATCH_CTA];
-    __shared__ uint32_t s_m[BATCH_CTA];
+    __shared__ uint32_t s_m[BATCH_CTA];   // elements of an operand (limbs or words)
+    __shared__ uint8_t s_w[BATCH_CTA];    // 1: 32-bit words
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(counter, 1u);
         __syncthreads();
@@ -116,6 +156,7 @@ batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
             s_b[i] = d.b;
             s_r[i] = d.r;
             s_m[i] = d.m;
+            s_w[i] = desc_w32(d) ? 1 : 0;
         }
         uint32_t cap = item.count;
         const MulGeom g0 = mul_geometry(item.Lp, item.full != 0, cap);
@@ -129,14 +170,15 @@ batch_mul_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
         for (uint32_t base = 0; base < item.count; base += g.ipc) {
             auto load = [&](uint32_t li, uint32_t x, uint64_t& va, uint64_t& vb) {
                 const uint32_t k = base + li;
-                if (k >= item.count || x >= s_m[k]) return;
-                va = in[s_a[k] + x];
-                vb = in[s_b[k] + x];
+                if (k >= item.count) return;
+                const bool w = s_w[k] != 0;
+                va = ld64(in, s_a[k], s_m[k], w, x);
+                vb = ld64(in, s_b[k], s_m[k], w, x);
             };
             auto store = [&](uint32_t li, uint32_t x, uint64_t v) {
                 const uint32_t k = base + li;
                 if (k >= item.count) return;
-                if (x < (full ? 2 * s_m[k] : s_m[k])) out[s_r[k] + x] = v;
+                st64(out, s_r[k], full ? 2 * s_m[k] : s_m[k], s_w[k] != 0, x, v);
             };
             mul_cta<MUL_C>(g, smem, scratch, lpdiv, load, store);
         }
@@ -164,19 +206,17 @@ batch_mulwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restri
         const uint32_t idx = idx0 + lg;
         bi_desc d = {};                       // a group past the list: m = 0, loads zeros, stores nothing
         if (idx < count) d = descs[list[idx]];
-        const uint64_t* pa = in + d.a;
-        const uint64_t* pb = in + d.b;
-        uint64_t* pr = out + d.r;
-        const uint32_t words = 2 * d.m;
+        const bool w32 = desc_w32(d);
+        const uint32_t words = w32 ? d.m : 2 * d.m;   // 32-bit words of an operand
+        const uint32_t* pa = reinterpret_cast<const uint32_t*>(in) + (w32 ? d.a : 2 * d.a);
+        const uint32_t* pb = reinterpret_cast<const uint32_t*>(in) + (w32 ? d.b : 2 * d.b);
         mul_warp_group<G>(
             sw, t, lg * G,
             [&](uint32_t x, uint32_t& wa, uint32_t& wb) {
-                wa = x < words ? (uint32_t)(pa[x >> 1] >> (32 * (x & 1))) : 0u;
-                wb = x < words ? (uint32_t)(pb[x >> 1] >> (32 * (x & 1))) : 0u;
+                wa = x < words ? pa[x] : 0u;
+                wb = x < words ? pb[x] : 0u;
             },
-            [&](uint32_t c, uint64_t v) {
-                if (c < 2 * d.m) pr[c] = v;
-            });
+            [&](uint32_t c, uint64_t v) { st64(out, d.r, 2 * d.m, w32, c, v); });
     }
 }
 
@@ -217,13 +257,13 @@ batch_divthread_kernel(const bi_desc* __restrict__ descs, const uint32_t* __rest
         const uint32_t idx = base + lane;
         if (idx >= count) continue;
         const bi_desc d = descs[list[idx]];
-        const uint64_t* u = in + d.a;
-        const uint64_t* v = in + d.b;
-        uint64_t* q = out + d.r;
-        uint64_t* r = out + d.r2;
+        const bool w32 = desc_w32(d);
+        auto lu = [&](uint32_t i) { return ld64(in, d.a, d.m, w32, i); };
+        auto lv = [&](uint32_t i) { return ld64(in, d.b, d.mb, w32, i); };
+        auto sq = [&](uint32_t i, uint64_t x) { st64(out, d.r, d.m, w32, i, x); };
+        auto sr = [&](uint32_t i, uint64_t x) { st64(out, d.r2, d.mb, w32, i, x); };
         const uint8_t st = div_thread<MX>(
-            d.m, d.mb, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
-            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; });
+            m64(d), mb64(d), lu, lv, sq, sr);
         if (flags) flags[d.flag] = st;
     }
 }
@@ -239,13 +279,13 @@ batch_divwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restri
         idx = __shfl_sync(0xffffffffu, idx, 0);
         if (idx >= count) break;
         const bi_desc d = descs[list[idx]];
-        const uint64_t* u = in + d.a;
-        const uint64_t* v = in + d.b;
-        uint64_t* q = out + d.r;
-        uint64_t* r = out + d.r2;
+        const bool w32 = desc_w32(d);
+        auto lu = [&](uint32_t i) { return ld64(in, d.a, d.m, w32, i); };
+        auto lv = [&](uint32_t i) { return ld64(in, d.b, d.mb, w32, i); };
+        auto sq = [&](uint32_t i, uint64_t x) { st64(out, d.r, d.m, w32, i, x); };
+        auto sr = [&](uint32_t i, uint64_t x) { st64(out, d.r2, d.mb, w32, i, x); };
         const uint8_t st = div_warp<VPL>(
-            d.m, d.mb, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
-            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; });
+            m64(d), mb64(d), lu, lv, sq, sr);
         if (flags && lane == 0) flags[d.flag] = st;
     }
 }
@@ -267,14 +307,13 @@ batch_divgroup_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restr
         const bool valid = idx < count;
         bi_desc d = {};
         if (valid) d = descs[list[idx]];
-        const uint64_t* u = in + d.a;
-        const uint64_t* v = in + d.b;
-        uint64_t* q = out + d.r;
-        uint64_t* r = out + d.r2;
+        const bool w32 = desc_w32(d);
+        auto lu = [&](uint32_t i) { return ld64(in, d.a, d.m, w32, i); };
+        auto lv = [&](uint32_t i) { return ld64(in, d.b, d.mb, w32, i); };
+        auto sq = [&](uint32_t i, uint64_t x) { st64(out, d.r, d.m, w32, i, x); };
+        auto sr = [&](uint32_t i, uint64_t x) { st64(out, d.r2, d.mb, w32, i, x); };
         const uint8_t st = div_group<VPL, G>(
-            valid, valid ? d.m : 1u, valid ? d.mb : 1u, [&](uint32_t i) { return u[i]; },
-            [&](uint32_t i) { return v[i]; }, [&](uint32_t i, uint64_t x) { q[i] = x; },
-            [&](uint32_t i, uint64_t x) { r[i] = x; });
+            valid, valid ? m64(d) : 1u, valid ? mb64(d) : 1u, lu, lv, sq, sr);
         if (flags && valid && (lane & (G - 1)) == 0) flags[d.flag] = st;
     }
 }
@@ -293,14 +332,14 @@ batch_div_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__
         __syncthreads();
         if (idx >= count) break;
         const bi_desc d = descs[list[idx]];
-        const DivGeom g = div_geom(d.m, d.mb, 8);
-        const uint64_t* u = in + d.a;
-        const uint64_t* v = in + d.b;
-        uint64_t* q = out + d.r;
-        uint64_t* r = out + d.r2;
+        const DivGeom g = div_geom(m64(d), mb64(d), 8);
+        const bool w32 = desc_w32(d);
+        auto lu = [&](uint32_t i) { return ld64(in, d.a, d.m, w32, i); };
+        auto lv = [&](uint32_t i) { return ld64(in, d.b, d.mb, w32, i); };
+        auto sq = [&](uint32_t i, uint64_t x) { st64(out, d.r, d.m, w32, i, x); };
+        auto sr = [&](uint32_t i, uint64_t x) { st64(out, d.r2, d.mb, w32, i, x); };
         div_cta(
-            g, smem, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
-            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; },
+            g, smem, lu, lv, sq, sr,
             [&](uint8_t code) { if (flags) flags[d.flag] = code; });
     }
 }
@@ -341,13 +380,13 @@ batch_divblk_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restric
         __syncthreads();
         if (idx >= count) break;
         const bi_desc d = descs[list[idx]];
-        const uint64_t* u = in + d.a;
-        const uint64_t* v = in + d.b;
-        uint64_t* q = out + d.r;
-        uint64_t* r = out + d.r2;
+        const bool w32 = desc_w32(d);
+        auto lu = [&](uint32_t i) { return ld64(in, d.a, d.m, w32, i); };
+        auto lv = [&](uint32_t i) { return ld64(in, d.b, d.mb, w32, i); };
+        auto sq = [&](uint32_t i, uint64_t x) { st64(out, d.r, d.m, w32, i, x); };
+        auto sr = [&](uint32_t i, uint64_t x) { st64(out, d.r2, d.mb, w32, i, x); };
         const uint8_t st = div_blk<32, 8, NW>(
-            d.m, d.mb, [&](uint32_t i) { return u[i]; }, [&](uint32_t i) { return v[i]; },
-            [&](uint32_t i, uint64_t x) { q[i] = x; }, [&](uint32_t i, uint64_t x) { r[i] = x; }, &sh);
+            m64(d), mb64(d), lu, lv, sq, sr, &sh);
         if (flags && threadIdx.x == 0) flags[d.flag] = st;
     }
 }
@@ -410,9 +449,9 @@ static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n,
     uint64_t cnt[DIV_CLASSES] = {};
     uint32_t max_m[DIV_CLASSES] = {};
     for (uint32_t k = 0; k < n; k++) {
-        const int c = div_class(descs[div[k]].mb);
+        const int c = div_class(mb64(descs[div[k]]));
         cnt[c]++;
-        max_m[c] = std::max(max_m[c], descs[div[k]].m);
+        max_m[c] = std::max(max_m[c], m64(descs[div[k]]));
     }
     for (int c = 0; c < DIV_CLASSES; c++) {
         map[c] = c;
@@ -428,9 +467,9 @@ static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n,
 
 // Division order: by class, then most expensive first.
 static bool div_before(const bi_desc& x, const bi_desc& y, const int* map) {
-    const int cx = map[div_class(x.mb)], cy = map[div_class(y.mb)];
+    const int cx = map[div_class(mb64(x))], cy = map[div_class(mb64(y))];
     if (cx != cy) return cx < cy;
-    return (uint64_t)x.m * x.mb > (uint64_t)y.m * y.mb;
+    return (uint64_t)m64(x) * mb64(x) > (uint64_t)m64(y) * mb64(y);
 }
 
 // Per-class offsets, counts and shared memory of a division list sorted by div_before.
@@ -443,9 +482,9 @@ static void div_classes(bi_plan* p, const bi_desc* descs, const uint32_t* div, u
     }
     for (uint32_t k = 0; k < n; k++) {
         const bi_desc& d = descs[div[k]];
-        const int c = map[div_class(d.mb)];
+        const int c = map[div_class(mb64(d))];
         if (p->n_divc[c]++ == 0) p->div_off[c] = k;
-        if (c == DIV_CTA_CLASS) p->divc_smem[c] = std::max(p->divc_smem[c], div_smem_bytes(div_geom(d.m, d.mb, 8)));
+        if (c == DIV_CTA_CLASS) p->divc_smem[c] = std::max(p->divc_smem[c], div_smem_bytes(div_geom(m64(d), mb64(d), 8)));
         p->div_smem = std::max(p->div_smem, p->divc_smem[c]);
     }
 }
@@ -692,8 +731,16 @@ static void plan_free(bi_plan* p) {
 static bi_status check_desc(const bi_desc& d, uint64_t i, uint64_t in_limbs, uint64_t out_limbs, uint64_t nflags) {
     const unsigned long long k = (unsigned long long)i;
     if (d.m == 0) return set_error(BI_EINVAL, "descriptor %llu: m=0", k);
-    if (d.op == BI_OP_DIV ? (d.m > BATCH_DIV_MAX_M || d.mb > BATCH_DIV_MAX_MB) : d.m > BATCH_MAX_LIMBS)
+    if (d.width != 0 && d.width != 32 && d.width != 64)
+        return set_error(BI_EINVAL, "descriptor %llu: width %u (0, 32 or 64)", k, d.width);
+    const bool w32 = desc_w32(d);
+    if (d.op == BI_OP_DIV ? (m64(d) > BATCH_DIV_MAX_M || mb64(d) > BATCH_DIV_MAX_MB) : m64(d) > BATCH_MAX_LIMBS)
         return set_error(BI_EUNSUPPORTED, "descriptor %llu: m=%u mb=%u above the batch's limits", k, d.m, d.mb);
+    // the arenas in the descriptor's elements
+    if (w32) {
+        in_limbs *= 2;
+        out_limbs *= 2;
+    }
     auto inside = [](uint64_t off, uint64_t len, uint64_t size) { return off <= size && len <= size - off; };
     uint64_t la = d.m, lb = d.m, lr = d.m, lr2 = 0;
     bool flag = false;
@@ -702,7 +749,7 @@ static bi_status check_desc(const bi_desc& d, uint64_t i, uint64_t in_limbs, uin
     case BI_OP_SUB: flag = true; break;
     case BI_OP_MUL: break;
     case BI_OP_MULFULL: {
-        const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
+        const uint32_t Lp = (m64(d) + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
         if (Lp > 2048) return set_error(BI_EUNSUPPORTED, "descriptor %llu: mulfull m=%u", k, d.m);
         lr = 2ull * d.m;
         break;
@@ -754,12 +801,12 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
             break;
         case BI_OP_MUL:
         case BI_OP_MULFULL: {
-            const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
+            const uint32_t Lp = (m64(d) + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
             const uint32_t full = d.op == BI_OP_MULFULL;
             if (full) p->max_mul_Lp_full = std::max(p->max_mul_Lp_full, Lp);
             else p->max_mul_Lp_trunc = std::max(p->max_mul_Lp_trunc, Lp);
             mulkeys.push_back({((uint64_t)full << 40) | ((uint64_t)Lp << 8), (uint32_t)i});
-            if (full && d.m <= MULW_MAX_M) mulw[mulw_class(d.m)].push_back((uint32_t)i);
+            if (full && m64(d) <= MULW_MAX_M) mulw[mulw_class(m64(d))].push_back((uint32_t)i);
             break;
         }
         default:   // BI_OP_DIV (check_desc refused every other op)
@@ -768,7 +815,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
         }
     }
     // largest first: long instances start early, short ones fill the tail
-    std::stable_sort(addsub.begin(), addsub.end(), [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
+    std::stable_sort(addsub.begin(), addsub.end(), [&](uint32_t x, uint32_t y) { return m64(descs[x]) > m64(descs[y]); });
     int dmap[DIV_CLASSES];
     div_class_map(descs, div.data(), (uint32_t)div.size(), num_sms(), dmap);
     std::stable_sort(div.begin(), div.end(), [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y], dmap); });
@@ -799,7 +846,7 @@ bi_status bi_plan_create(bi_plan** out_plan, const bi_desc* descs, uint64_t coun
     // the warp classes' lists, largest first within a class, one after another
     std::vector<uint32_t> mulw_all;
     for (int c = 0; c < MULW_CLASSES; c++) {
-        std::stable_sort(mulw[c].begin(), mulw[c].end(), [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
+        std::stable_sort(mulw[c].begin(), mulw[c].end(), [&](uint32_t x, uint32_t y) { return m64(descs[x]) > m64(descs[y]); });
         p->mulw_off[c] = (uint32_t)mulw_all.size();
         p->n_mulw[c] = (uint32_t)mulw[c].size();
         mulw_all.insert(mulw_all.end(), mulw[c].begin(), mulw[c].end());
@@ -1092,7 +1139,7 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
         if (d.op == BI_OP_ADD || d.op == BI_OP_SUB) {
             na_add[na++] = (uint32_t)i;
         } else if (d.op == BI_OP_MUL || d.op == BI_OP_MULFULL) {
-            const uint32_t Lp = (d.m + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
+            const uint32_t Lp = (m64(d) + 2 * MUL_C - 1) / (2 * MUL_C) * (2 * MUL_C);
             const uint32_t full = d.op == BI_OP_MULFULL;
             if (full) p.max_mul_Lp_full = std::max(p.max_mul_Lp_full, Lp);
             else p.max_mul_Lp_trunc = std::max(p.max_mul_Lp_trunc, Lp);
@@ -1101,7 +1148,7 @@ extern "C" bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count, 
             na_div[nd++] = (uint32_t)i;
         }
     }
-    std::stable_sort(na_add, na_add + na, [&](uint32_t x, uint32_t y) { return descs[x].m > descs[y].m; });
+    std::stable_sort(na_add, na_add + na, [&](uint32_t x, uint32_t y) { return m64(descs[x]) > m64(descs[y]); });
     int dmap[DIV_CLASSES];
     div_class_map(descs, na_div, nd, num_sms(), dmap);
     std::stable_sort(na_div, na_div + nd, [&](uint32_t x, uint32_t y) { return div_before(descs[x], descs[y], dmap); });

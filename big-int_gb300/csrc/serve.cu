@@ -446,7 +446,7 @@ static bi_status server_admit(bi_server* s, const bi_desc* req, uint64_t* ticket
     d.r = off;
     d.r2 = off + d.m;
     d.flag = 0;
-    d.reserved = 0;
+    d.width = 0;
     const uint64_t seq = s->published;
     ServeReq& q = s->req[seq & (s->S - 1)];
     q.seq = seq;

@@ -306,13 +306,18 @@ bi_status bi_limbs_to_words(const uint64_t* limbs, uint32_t m, size_t size,
 
 typedef struct bi_desc {
     uint32_t op;        /* BI_OP_* */
-    uint32_t m;         /* limbs of a (the dividend for BI_OP_DIV) */
-    uint32_t mb;        /* limbs of b for BI_OP_DIV (1 <= mb <= m); else ignored (= m) */
-    uint32_t reserved;  /* 0 */
-    uint64_t a, b;      /* limb offsets of the operands in the input arena */
-    uint64_t r, r2;     /* limb offsets of the results in the output arena */
+    uint32_t m;         /* elements of a (the dividend for BI_OP_DIV) */
+    uint32_t mb;        /* elements of b for BI_OP_DIV (1 <= mb <= m); else ignored (= m) */
+    uint32_t width;     /* element width: 0 or 64 = 64-bit limbs; 32 = 32-bit words */
+    uint64_t a, b;      /* element offsets of the operands in the input arena */
+    uint64_t r, r2;     /* element offsets of the results in the output arena */
     uint64_t flag;      /* byte offset of the sign / status in the flag arena */
 } bi_desc;
+/* With width = 32 the instance is the reference's U32bits layout: m, mb   */
+/* and the offsets count 32-bit words of the same arenas (word k of an     */
+/* arena of 64-bit limbs is the low half of limb k/2 for even k), so a    */
+/* batch can mix 32-bit-word and 64-bit-limb instances.  Size limits are  */
+/* the same in bits: twice as many words as limbs.                        */
 
 typedef struct bi_plan bi_plan;
 

@@ -352,3 +352,80 @@ def test_batch_size_limits_rejected(bigint):
             B.Plan(d, 1 << 20, 1 << 20, 16)
         assert ei.value.status == 6             # BI_EUNSUPPORTED
 
+
+
+def _mixed_width_batch(B, n=1200, seed=55):
+    """A batch mixing 64-bit-limb instances (width 0) and 32-bit-word ones
+    (width 32) of every op: odd and even word counts, odd and even word
+    offsets, all-ones operands, divisors of every class up to 1100 words."""
+    rng = np.random.default_rng(seed)
+    ops = [B.OP_ADD, B.OP_SUB, B.OP_MUL, B.OP_MULFULL, B.OP_DIV]
+    d = np.zeros(n, dtype=B.DESC_DTYPE)
+    pos64 = out64 = 0
+    rows = []
+    for i in range(n):
+        op = ops[i % 5]
+        w32 = (i // 5) % 3 != 0
+        m = int(rng.integers(1, 2200 if op == B.OP_DIV else 300))
+        if op == B.OP_MULFULL and i % 7 == 0:
+            m = int(rng.integers(1, 65))                 # the warp-multiply classes
+        mb = int(rng.integers(1, m + 1)) if op == B.OP_DIV else m
+        rows.append((op, m, mb, w32))
+    # 64-bit instances first (limb offsets), then the word instances (word offsets, some odd)
+    for i, (op, m, mb, w32) in enumerate(rows):
+        if w32:
+            continue
+        d[i]["op"], d[i]["m"], d[i]["mb"], d[i]["width"] = op, m, mb, 0
+        d[i]["a"], d[i]["b"] = pos64, pos64 + m
+        pos64 += m + mb
+        d[i]["r"] = out64
+        out64 += 2 * m if op == B.OP_MULFULL else m
+        if op == B.OP_DIV:
+            d[i]["r2"] = out64
+            out64 += mb
+    pw, ow = 2 * pos64 + 1, 2 * out64 + 3               # word cursors, starting odd
+    for i, (op, m, mb, w32) in enumerate(rows):
+        if not w32:
+            continue
+        d[i]["op"], d[i]["m"], d[i]["mb"], d[i]["width"] = op, m, mb, 32
+        d[i]["a"], d[i]["b"] = pw, pw + m
+        pw += m + mb + (i & 1)
+        d[i]["r"] = ow
+        ow += 2 * m if op == B.OP_MULFULL else m
+        if op == B.OP_DIV:
+            d[i]["r2"] = ow
+            ow += mb
+        ow += i & 1
+    d["flag"] = np.arange(n)
+    in_limbs, out_limbs = (pw + 1) // 2 + 1, (ow + 1) // 2 + 1
+    arena = rng.integers(0, 2**64, size=in_limbs, dtype=np.uint64)
+    a32 = arena.view(np.uint32)
+    for i, (op, m, mb, w32) in enumerate(rows):
+        view, off = (a32, int(d[i]["b"])) if w32 else (arena, int(d[i]["b"]))
+        if op == B.OP_DIV:
+            view[off + mb - 1] |= view.dtype.type(1)    # nonzero top divisor element
+        if i % 11 == 0:                                  # all-ones operands
+            oa = int(d[i]["a"])
+            view[oa: oa + m] = np.iinfo(view.dtype).max
+    return d, arena, out_limbs, n
+
+
+def test_mixed_width_batch_matches_oracle(bigint, oracle):
+    """32-bit-word instances (the reference's U32bits layout) in the same
+    batch as 64-bit-limb ones, each checked against the oracle on its own
+    element type."""
+    import os
+
+    import torch
+
+    B = bigint
+    d, arena, out_limbs, nflags = _mixed_width_batch(B)
+    plan, din, dout, dfl = _run(B, d, arena, out_limbs, nflags)
+    out = B.to_host(dout, np.uint64)
+    flags = dfl.cpu().numpy()
+    th = os.cpu_count() or 1
+    for w, a_view, o_view in ((0, arena, out), (32, arena.view(np.uint32), out.view(np.uint32))):
+        sel = np.nonzero(d["width"] == w)[0]
+        assert sel.size > 100
+        check_batch(B, oracle, d[sel], a_view, o_view, flags, nthreads=th)
+    plan.close()
