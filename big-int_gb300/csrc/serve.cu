@@ -32,6 +32,7 @@
 #include <cstring>
 #include <vector>
 
+#include "descio.cuh"
 #include "divcore.cuh"
 #include "divsmall.cuh"
 #include "mulcore.cuh"
@@ -215,55 +216,59 @@ __global__ void __launch_bounds__(SERVE_CTA, 2) serve_kernel(const ServeArgs A) 
         if (cmd == CLAIM_EXIT) break;
         if (cmd == CLAIM_OK) {
             const bi_desc d = s_d;
-            const uint64_t* a = A.in + d.a;
-            const uint64_t* b = A.in + d.b;
-            uint64_t* r = A.out + d.r;
+            const bool w32 = desc_w32(d);
+            const uint32_t M = m64(d), MB = mb64(d);   // sizes in 64-bit limbs
             if (d.op == BI_OP_ADD || d.op == BI_OP_SUB) {
                 if (threadIdx.x < 32) {
                     const bool sub = d.op == BI_OP_SUB;
-                    // 16-byte accesses need even limb offsets (the arenas are 16-byte aligned)
-                    if (((d.a | d.b | d.r) & 1ull) == 0)
-                        warp_addsub<2, 4>(a, b, r, &s_sign, d.m, sub);
-                    else
-                        warp_addsub<1, 4>(a, b, r, &s_sign, d.m, sub);
+                    if (w32 && ((d.a | d.b | d.r | d.m) & 1ull) != 0) {   // words that do not pair into limbs
+                        const uint32_t* in32 = reinterpret_cast<const uint32_t*>(A.in);
+                        warp_addsub<1, 4, uint32_t>(in32 + d.a, in32 + d.b, reinterpret_cast<uint32_t*>(A.out) + d.r,
+                                                    &s_sign, d.m, sub);
+                    } else {
+                        const uint64_t a = w32 ? d.a / 2 : d.a, b = w32 ? d.b / 2 : d.b, r = w32 ? d.r / 2 : d.r;
+                        // 16-byte accesses need even limb offsets (the arenas are 16-byte aligned)
+                        if (((a | b | r) & 1ull) == 0)
+                            warp_addsub<2, 4>(A.in + a, A.in + b, A.out + r, &s_sign, M, sub);
+                        else
+                            warp_addsub<1, 4>(A.in + a, A.in + b, A.out + r, &s_sign, M, sub);
+                    }
                     if (threadIdx.x == 0 && sub) s_flag = s_sign;
                 }
             } else if (d.op == BI_OP_MUL || d.op == BI_OP_MULFULL) {
                 const bool full = d.op == BI_OP_MULFULL;
-                const MulGeom g = mul_geometry_single_sliced(d.m, full, SERVE_CTA);
+                const MulGeom g = mul_geometry_single_sliced(M, full, SERVE_CTA);
                 uint32_t* scratch = reinterpret_cast<uint32_t*>(smem + (size_t)g.ipc * g.IS);
                 const FastDiv lpdiv(g.Lp);
-                const uint32_t m = d.m, outl = full ? 2 * d.m : d.m;
+                const uint32_t outn = full ? 2 * d.m : d.m;   // result elements
                 auto load = [&](uint32_t, uint32_t x, uint64_t& va, uint64_t& vb) {
-                    if (x < m) { va = a[x]; vb = b[x]; }
+                    va = ld64(A.in, d.a, d.m, w32, x);
+                    vb = ld64(A.in, d.b, d.m, w32, x);
                 };
-                auto store = [&](uint32_t, uint32_t x, uint64_t v) {
-                    if (x < outl) r[x] = v;
-                };
+                auto store = [&](uint32_t, uint32_t x, uint64_t v) { st64(A.out, d.r, outn, w32, x, v); };
                 mul_cta<MUL_C>(g, smem, scratch, lpdiv, load, store);
             } else {   // BI_OP_DIV (the host admits nothing else)
-                uint64_t* r2 = A.out + d.r2;
-                auto ld_u = [&](uint32_t i) { return a[i]; };
-                auto ld_v = [&](uint32_t i) { return b[i]; };
-                auto st_q = [&](uint32_t i, uint64_t x) { r[i] = x; };
-                auto st_r = [&](uint32_t i, uint64_t x) { r2[i] = x; };
+                auto ld_u = [&](uint32_t i) { return ld64(A.in, d.a, d.m, w32, i); };
+                auto ld_v = [&](uint32_t i) { return ld64(A.in, d.b, d.mb, w32, i); };
+                auto st_q = [&](uint32_t i, uint64_t x) { st64(A.out, d.r, d.m, w32, i, x); };
+                auto st_r = [&](uint32_t i, uint64_t x) { st64(A.out, d.r2, d.mb, w32, i, x); };
                 // long division on one thread or one warp where it finishes
                 // sooner than the CTA's shifted inverse (divsmall.cuh)
-                if (d.mb <= SERVE_DIV_THREAD_MAX_MV) {
+                if (MB <= SERVE_DIV_THREAD_MAX_MV) {
                     if (threadIdx.x == 0) {
-                        const uint8_t st = d.mb <= 4 ? div_thread<4>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
-                                                     : div_thread<8>(d.m, d.mb, ld_u, ld_v, st_q, st_r);
+                        const uint8_t st = MB <= 4 ? div_thread<4>(M, MB, ld_u, ld_v, st_q, st_r)
+                                                   : div_thread<8>(M, MB, ld_u, ld_v, st_q, st_r);
                         s_flag = st;
                     }
-                } else if (d.mb <= SERVE_DIV_WARP_MAX_MV) {
+                } else if (MB <= SERVE_DIV_WARP_MAX_MV) {
                     if (threadIdx.x < 32) {
-                        const uint8_t st = d.mb <= 32 ? div_warp<1>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
-                                                      : d.mb <= 64 ? div_warp<2>(d.m, d.mb, ld_u, ld_v, st_q, st_r)
-                                                                   : div_warp<4>(d.m, d.mb, ld_u, ld_v, st_q, st_r);
+                        const uint8_t st = MB <= 32 ? div_warp<1>(M, MB, ld_u, ld_v, st_q, st_r)
+                                                    : MB <= 64 ? div_warp<2>(M, MB, ld_u, ld_v, st_q, st_r)
+                                                               : div_warp<4>(M, MB, ld_u, ld_v, st_q, st_r);
                         if (threadIdx.x == 0) s_flag = st;
                     }
                 } else {
-                    const DivGeom g = div_geom(d.m, d.mb, 8);
+                    const DivGeom g = div_geom(M, MB, 8);
                     div_cta(g, smem, ld_u, ld_v, st_q, st_r, [&](uint8_t code) { s_flag = code; });
                 }
             }
@@ -288,17 +293,22 @@ static uint64_t now_ns() {
         .count();
 }
 
+// Output-arena limbs a request's results take: whole 64-bit limbs, an even
+// number of them so that every result starts 16-byte aligned.
 static uint64_t result_limbs(const bi_desc& d) {
+    uint64_t e;   // result elements
     switch (d.op) {
-        case BI_OP_MULFULL: return 2ull * d.m;
-        case BI_OP_DIV: return (uint64_t)d.m + d.mb;
-        default: return d.m;
+        case BI_OP_MULFULL: e = 2ull * d.m; break;
+        case BI_OP_DIV: e = (uint64_t)d.m + d.mb; break;
+        default: e = d.m;
     }
+    const uint64_t limbs = desc_w32(d) ? (e + 1) / 2 : e;
+    return (limbs + 1) & ~1ull;
 }
 
 static size_t request_smem(const bi_desc& d) {
-    if (d.op == BI_OP_MUL || d.op == BI_OP_MULFULL) return mul_smem_bytes(mul_geometry(d.m, d.op == BI_OP_MULFULL, 1));
-    if (d.op == BI_OP_DIV) return div_smem_bytes(div_geom(d.m, d.mb, 8));
+    if (d.op == BI_OP_MUL || d.op == BI_OP_MULFULL) return mul_smem_bytes(mul_geometry(m64(d), d.op == BI_OP_MULFULL, 1));
+    if (d.op == BI_OP_DIV) return div_smem_bytes(div_geom(m64(d), mb64(d), 8));
     return 0;
 }
 
@@ -415,13 +425,15 @@ static bi_status server_validate(const bi_server* s, const bi_desc& req) {
     bi_desc d = req;
     if (d.op > BI_OP_DIV) return set_error(BI_EINVAL, "serve: unknown op %u", d.op);
     if (d.op != BI_OP_DIV) d.mb = d.m;
-    if (d.m == 0 || d.m > s->max_limbs)
-        return set_error(BI_EINVAL, "serve: m=%u outside 1..%u (the server's max_limbs)", d.m, s->max_limbs);
+    if (d.width != 0 && d.width != 32 && d.width != 64) return set_error(BI_EINVAL, "serve: width %u (0, 32 or 64)", d.width);
+    if (d.m == 0 || m64(d) > s->max_limbs)
+        return set_error(BI_EINVAL, "serve: m=%u outside the server's max_limbs (%u 64-bit limbs)", d.m, s->max_limbs);
     if (d.mb == 0 || d.mb > d.m) return set_error(BI_EINVAL, "serve: divisor limbs mb=%u outside 1..m", d.mb);
-    if (d.a > s->in_limbs || d.m > s->in_limbs - d.a || d.b > s->in_limbs || d.mb > s->in_limbs - d.b)
+    const uint64_t in_elems = desc_w32(d) ? 2 * s->in_limbs : s->in_limbs;
+    if (d.a > in_elems || d.m > in_elems - d.a || d.b > in_elems || d.mb > in_elems - d.b)
         return set_error(BI_EINVAL, "serve: operand outside the operand arena");
     if (request_smem(d) > s->smem) return set_error(BI_EUNSUPPORTED, "serve: request needs more shared memory than the loop holds");
-    if (((result_limbs(d) + 1) & ~1ull) > s->out_limbs) return set_error(BI_EINVAL, "serve: result larger than the output arena");
+    if (result_limbs(d) > s->out_limbs) return set_error(BI_EINVAL, "serve: result larger than the output arena");
     return BI_OK;
 }
 
@@ -434,7 +446,7 @@ static bi_status server_admit(bi_server* s, const bi_desc* req, uint64_t* ticket
         s->busy++;
         return BI_EBUSY;
     }
-    const uint64_t need = (result_limbs(d) + 1) & ~1ull;
+    const uint64_t need = result_limbs(d);
     const uint64_t pos = s->alloc_head % s->out_limbs;
     const uint64_t skip = pos + need > s->out_limbs ? s->out_limbs - pos : 0;
     if (s->alloc_head + skip + need - s->alloc_tail > s->out_limbs) {
@@ -443,10 +455,9 @@ static bi_status server_admit(bi_server* s, const bi_desc* req, uint64_t* ticket
     }
     const uint64_t off = (s->alloc_head + skip) % s->out_limbs;
     s->alloc_head += skip + need;
-    d.r = off;
-    d.r2 = off + d.m;
+    d.r = desc_w32(d) ? 2 * off : off;   // in the request's elements
+    d.r2 = d.r + d.m;
     d.flag = 0;
-    d.width = 0;
     const uint64_t seq = s->published;
     ServeReq& q = s->req[seq & (s->S - 1)];
     q.seq = seq;
@@ -719,7 +730,9 @@ bi_status bi_serve_replay_plain(const uint64_t* in, uint64_t* out, uint64_t out_
     out_limbs &= ~1ull;
     for (uint64_t i = 0; i < n; i++) {
         if (reqs[i].op > BI_OP_DIV || reqs[i].m == 0) return set_error(BI_EINVAL, "serve: bad request %llu", (unsigned long long)i);
-        if (result_limbs(reqs[i]) + 1 > out_limbs) return set_error(BI_EINVAL, "serve: output arena too small");
+        if (reqs[i].width != 0 && reqs[i].width != 32 && reqs[i].width != 64)
+            return set_error(BI_EINVAL, "serve: bad request %llu", (unsigned long long)i);
+        if (result_limbs(reqs[i]) > out_limbs) return set_error(BI_EINVAL, "serve: output arena too small");
         if (i && arrival_ns[i] < arrival_ns[i - 1]) return set_error(BI_EINVAL, "serve: arrival times must not decrease");
     }
     constexpr uint32_t EV_PER_STREAM = 1024;
@@ -768,20 +781,35 @@ bi_status bi_serve_replay_plain(const uint64_t* in, uint64_t* out, uint64_t out_
             Lane& l = lanes[launched % streams];
             if (l.tail - l.head >= EV_PER_STREAM) break;
             const bi_desc& d = reqs[launched];
-            const uint64_t need = (result_limbs(d) + 1) & ~1ull;
+            const uint64_t need = result_limbs(d);
             if (alloc % out_limbs + need > out_limbs) alloc += out_limbs - alloc % out_limbs;
             const uint64_t off = alloc % out_limbs;
             alloc += need;
-            r_off[launched] = off;
-            r2_off[launched] = d.op == BI_OP_DIV ? off + d.m : 0;
+            const bool w32 = desc_w32(d);
+            const uint64_t ro = w32 ? 2 * off : off;   // in the request's elements
+            r_off[launched] = ro;
+            r2_off[launched] = d.op == BI_OP_DIV ? ro + d.m : 0;
             const bi_stream st = (bi_stream)l.st;
-            switch (d.op) {
-                case BI_OP_ADD: result = bi_add_u64(in + d.a, in + d.b, out + off, d.m, 1, st); break;
-                case BI_OP_SUB: result = bi_sub_u64(in + d.a, in + d.b, out + off, flags + launched, d.m, 1, st); break;
-                case BI_OP_MUL: result = bi_mul_u64(in + d.a, in + d.b, out + off, d.m, 1, st); break;
-                case BI_OP_MULFULL: result = bi_mulfull_u64(in + d.a, in + d.b, out + off, d.m, 1, st); break;
-                default:
-                    result = bi_div_u64(in + d.a, in + d.b, out + off, out + off + d.m, flags + launched, d.m, d.mb, 1, st);
+            if (w32) {
+                const uint32_t* i32 = reinterpret_cast<const uint32_t*>(in);
+                uint32_t* o32 = reinterpret_cast<uint32_t*>(out) + ro;
+                switch (d.op) {
+                    case BI_OP_ADD: result = bi_add_u32(i32 + d.a, i32 + d.b, o32, d.m, 1, st); break;
+                    case BI_OP_SUB: result = bi_sub_u32(i32 + d.a, i32 + d.b, o32, flags + launched, d.m, 1, st); break;
+                    case BI_OP_MUL: result = bi_mul_u32(i32 + d.a, i32 + d.b, o32, d.m, 1, st); break;
+                    case BI_OP_MULFULL: result = bi_mulfull_u32(i32 + d.a, i32 + d.b, o32, d.m, 1, st); break;
+                    default:
+                        result = bi_div_u32(i32 + d.a, i32 + d.b, o32, o32 + d.m, flags + launched, d.m, d.mb, 1, st);
+                }
+            } else {
+                switch (d.op) {
+                    case BI_OP_ADD: result = bi_add_u64(in + d.a, in + d.b, out + off, d.m, 1, st); break;
+                    case BI_OP_SUB: result = bi_sub_u64(in + d.a, in + d.b, out + off, flags + launched, d.m, 1, st); break;
+                    case BI_OP_MUL: result = bi_mul_u64(in + d.a, in + d.b, out + off, d.m, 1, st); break;
+                    case BI_OP_MULFULL: result = bi_mulfull_u64(in + d.a, in + d.b, out + off, d.m, 1, st); break;
+                    default:
+                        result = bi_div_u64(in + d.a, in + d.b, out + off, out + off + d.m, flags + launched, d.m, d.mb, 1, st);
+                }
             }
             if (result != BI_OK) break;
             const uint64_t e = l.tail % EV_PER_STREAM;

@@ -393,9 +393,11 @@ bi_status bi_batch_run_noalloc(const bi_desc* descs, uint64_t count,
 /* batching.  No counterpart in the reference (its benchmarks launch fixed */
 /* batches, cuda/main.cu:476-515).  A request is a bi_desc over the        */
 /* server's operand arena `in` (device, 16-byte aligned); the server fills */
-/* in r, r2 (limb offsets of the results in its output arena) and ignores  */
-/* flag.  64-bit limbs; m <= max_limbs for every op (the dividend's limbs  */
-/* for BI_OP_DIV, divisor 1 <= mb <= m).                                   */
+/* in r, r2 (offsets of the results in its output arena, in the request's */
+/* elements) and ignores flag.  A request's width says whether m, mb and  */
+/* the offsets count 64-bit limbs or 32-bit words; m in 64-bit limbs <=   */
+/* max_limbs for every op (the dividend for BI_OP_DIV, divisor 1 <= mb <= */
+/* m).                                                                     */
 /*                                                                         */
 /* Admission: a request enters when one of ring_slots slots and room for   */
 /* its results in the output arena (the HBM budget) are free; otherwise    */

@@ -321,3 +321,59 @@ def test_dropped_request_times_out_and_the_loop_goes_on(bigint, oracle, setup):
             _check_oracle(B, oracle, d[i: i + 1], host, res)
         for t in (t0, tl, t1):
             srv.release(t)
+
+
+def _word_requests(B, d, n=300):
+    """The stream's first n requests as 32-bit-word requests (width 32): odd
+    and even word counts, some at odd word offsets of the same pool."""
+    w = d[:n].copy()
+    for i in range(n):
+        m, mb = int(w["m"][i]), int(w["mb"][i])
+        mw = 2 * m - (i & 1)
+        mbw = min(mw, 2 * mb - ((i >> 1) & 1)) if int(w["op"][i]) == B.OP_DIV else mw
+        w[i]["m"], w[i]["mb"], w[i]["width"] = mw, mbw, 32
+        w[i]["a"] = 2 * int(w["a"][i]) + (1 if i % 3 == 0 else 0)
+        w[i]["b"] = 2 * int(w["b"][i]) + (1 if i % 5 == 0 else 0)
+    return w
+
+
+def _word_arena_limbs(B, d):
+    m = d["m"].astype(np.int64)
+    e = np.where(d["op"] == B.OP_MULFULL, 2 * m, np.where(d["op"] == B.OP_DIV, m + d["mb"], m))
+    limbs = (e + 1) // 2
+    return int(((limbs + 1) // 2 * 2).sum())
+
+
+def test_word_requests_match_oracle_and_plain(bigint, oracle, setup):
+    """32-bit-word requests (the reference's U32bits layout) through the
+    loop: results at word offsets equal the oracle's on the words and the
+    plain per-request launches' (bi_*_u32)."""
+    B = bigint
+    d, arrival, pool, host = setup
+    w = _word_requests(B, d)
+    h32 = host.view(np.uint32)
+    arena = _arena(_word_arena_limbs(B, w) + 16)
+    with B.Server(pool, arena) as srv:
+        lat, comp, rep = srv.replay(w, arrival[: len(w)])
+    assert rep["requests"] == len(w)
+    res = _collect(B, w, comp, _host(arena).view(np.uint32))
+    _check_oracle(B, oracle, w, h32, res)
+    arena2 = _arena(_word_arena_limbs(B, w) + 16)
+    _, comp2, _ = B.replay_plain(pool, arena2, w, arrival[: len(w)], streams=2)
+    _same(res, _collect(B, w, comp2, _host(arena2).view(np.uint32)))
+
+
+def test_word_request_checks(bigint, setup):
+    """A word request is checked in words: an operand past the pool's
+    2 x limbs words and a width other than 0, 32 or 64 are refused."""
+    B = bigint
+    d, _, pool, _ = setup
+    with B.Server(pool, _arena(1 << 16)) as srv:
+        bad = d[:1].copy()
+        bad[0]["width"], bad[0]["op"], bad[0]["m"] = 32, B.OP_ADD, 8
+        bad[0]["a"] = 2 * POOL - 7
+        with pytest.raises(B.BigIntError):
+            srv.submit(bad[0])
+        bad[0]["a"], bad[0]["width"] = 0, 16
+        with pytest.raises(B.BigIntError):
+            srv.submit(bad[0])
