@@ -140,7 +140,8 @@ bi_status bi_mul_set_tuning_u32(uint32_t m, int full, int ipc, int slices);
 /* correction bound exceeded (never observed).  The reference divides by   */
 /* zero (div.c:165-181); this entry reports it per instance instead.       */
 /* q and r must not overlap u, v or each other.                            */
-/* mu <= bi_max_limbs_div_* ().                                            */
+/* mu <= bi_max_limbs_div_* () (8192 64-bit limbs), mv <= 4096 64-bit    */
+/* limbs.                                                                  */
 /* ---------------------------------------------------------------------- */
 uint32_t bi_max_limbs_div_u64(void);
 uint32_t bi_max_limbs_div_u32(void);
@@ -153,11 +154,13 @@ bi_status bi_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t
 /* The method depends on the divisor's size in 64-bit limbs and on n (the */
 /* results do not: q and r are unique): schoolbook long division on one   */
 /* thread per instance up to 16 limbs and on one warp per instance up to  */
-/* 128 limbs, and up to 1024 limbs once n exceeds a few instances per SM; */
-/* otherwise the shifted inverse on one CTA per instance.  The _shinv     */
-/* entries take the shifted inverse at every size (the reference's        */
-/* algorithm), the _long entries long division (divisors up to 1024       */
-/* 64-bit limbs, else BI_EUNSUPPORTED); same arguments and results.       */
+/* 128 limbs, and up to 1024 limbs once n exceeds a few instances per SM  */
+/* (otherwise the shifted inverse on one CTA per instance); above 1024    */
+/* limbs long division 8 quotient limbs at a time on two or four warps.   */
+/* The _shinv entries take the shifted inverse at every size (the         */
+/* reference's algorithm; dividends up to 2048 64-bit limbs, else         */
+/* BI_EUNSUPPORTED), the _long entries long division (divisors up to 4096 */
+/* 64-bit limbs); same arguments and results.                             */
 bi_status bi_div_shinv_u64(const uint64_t* u, const uint64_t* v, uint64_t* q, uint64_t* r,
                            uint8_t* status, uint32_t mu, uint32_t mv, uint64_t n,
                            bi_stream stream);
