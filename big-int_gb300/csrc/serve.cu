@@ -45,9 +45,13 @@ constexpr uint32_t SERVE_MAX_LIMBS = 2048;       // largest operand (64-bit limb
 constexpr uint64_t SERVE_WAIT_NS = 1000000000;   // give up on a slot after 1 s
 constexpr uint64_t SERVE_LOST = 0xFF;            // status of a request whose slot never filled
 // divisors up to this many limbs divide on warp 0 (long division), larger ones
-// on the whole CTA (shifted inverse): measured on the serving workload, 64
-// (the single-division crossover) gave p90 40-45 us against 36-38 here
-constexpr uint32_t SERVE_DIV_WARP_MAX_MV = 128;
+// on the whole CTA (shifted inverse).  One division alone: 160/80 limbs 39 us
+// on a warp and 41 on a CTA, 192/96 47 and 41, 256/128 60 and 49.  On the
+// serving workload 64 gave p90 40-45 us against 36-38 at 128 (a CTA-wide
+// division slows the SM's other serving CTA), and 96 against 128 takes the
+// p99 of the 65..256-limb divisions from 61-65 to 55-62 us with the overall
+// p50 / p90 / p99 unchanged within 0.6 us (10k, 100k and 1M requests/s)
+constexpr uint32_t SERVE_DIV_WARP_MAX_MV = 96;
 // divisors up to this many limbs divide on thread 0: one division alone takes
 // 3.9 us on a thread and 4.3 on a warp at 8/4 limbs, 5.9 and 5.3 at 16/8,
 // 13.7 and 7.9 at 32/16 (GB300)
