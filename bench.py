@@ -425,7 +425,7 @@ def measure_extra(B, L, stream, args):
                           "note": "4096 pairs of 64 u32 limbs, 10% all-ones, full 128-limb product; a launch this "
                                   "short is timed as one replay of a CUDA graph of 20 launches (host overhead "
                                   "excluded, as for the reference kernel beside it)"}
-    # small full products (the warp-level path): 2^27 limbs of input per size, graph-timed
+    # small full products (the thread and warp kernels): 2^22 limbs of input per operand and size, graph-timed
     small = {}
     for m in (2, 4, 8, 16, 32):
         n = (1 << 22) // m
@@ -434,14 +434,15 @@ def measure_extra(B, L, stream, args):
         r = torch.empty((n, 2 * m), dtype=torch.int64, device="cuda")
         ms = graph_time(lambda st: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, st)), 5)
         wp = n * (2 * m) ** 2
-        # the autotuner weighs the warp kernel (32-bit words) against the CTA tilings (64-bit limbs)
+        # the autotuner weighs the thread and warp kernels against the CTA tilings (64-bit limbs)
         chosen = (ctypes.c_int * 2)()
         check(L, L.bi_mul_autotune_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, 1, 3,
                                        ctypes.cast(chosen, ctypes.c_void_p), sp))
         ms_tuned = graph_time(lambda st: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n,
                                                                     st)), 5)
         check(L, L.bi_mul_set_tuning_u64(m, 1, 0, 0))       # back to the library's own choice
-        pick = ("warp kernel, 32-bit words" if chosen[0] == 0 else
+        pick = ("warp kernel, 32-bit words" if (chosen[0], chosen[1]) == (0, 0) else
+                "thread kernel, 64-bit limbs" if (chosen[0], chosen[1]) == (0, 1) else
                 f"CTA kernel, 64-bit limbs, {chosen[0]} instances x {chosen[1]} slices")
         small[f"m{m}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "word_products_per_s": wp / ms * 1e3,
                                "frac_of_intpipe_peak": round(wp / ms * 1e3 / peak_wps, 4),

@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "mulcore.cuh"
+#include "multhread.cuh"
 #include "mulwarp.cuh"
 
 namespace bi {
@@ -139,8 +140,9 @@ mulchain_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict_
 
 // ---------------------------------------------------------------------------
 // Warp-level full product for small operands on 32-bit words (mulwarp.cuh):
-// the library routes full products of at most 64 32-bit words (32 64-bit
-// limbs) here, for both limb types, unless a CTA tiling was tuned for m.
+// the library routes full products of 25 to 32 64-bit limbs (49 to 64
+// 32-bit words) here, for both limb types, unless a tuning says otherwise;
+// smaller ones go to the thread kernel above.
 // ---------------------------------------------------------------------------
 
 // word x (32-bit) of operand row p with `words` words
@@ -211,9 +213,143 @@ static bi_status mul_warp(const T* a, const T* b, T* r, uint32_t m, uint64_t n, 
 }
 
 // ---------------------------------------------------------------------------
+// One thread per instance for full products of at most MUL_THREAD_MAX_L
+// 64-bit limbs (multhread.cuh): the library's default there, for both limb
+// types.  A CTA moves mul_thread_cta<M>() instances' operands into shared memory
+// with coalesced loads, each thread multiplies its own row in registers and
+// leaves the product in shared memory, and the CTA writes the tile back with
+// coalesced stores.  64-bit limbs (u64, and u32 batches of an even word count
+// on 8-byte-aligned buffers, which are the same bytes): rows at an odd stride
+// of P limbs, so that consecutive threads' 8-byte reads of their own rows hit
+// distinct banks.  u32 batches of an odd word count m = 2M - 1: the tile is
+// kept as the words arrive (row stride m, odd, so each thread's 32-bit reads
+// are conflict-free too) and the product at stride 2m words.
+// ---------------------------------------------------------------------------
+template <typename T, int M>
+__global__ void __launch_bounds__(mul_thread_cta<M>())
+mul_thread_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, uint64_t n, uint32_t m) {
+    constexpr uint32_t CT = mul_thread_cta<M>();
+    constexpr uint32_t P = (M % 2 == 0) ? M + 1 : M;    // operand row stride (limbs)
+    constexpr uint32_t Q = 2 * M + 1;                  // product row stride (limbs)
+    constexpr uint32_t S = (2 * P > Q ? 2 * P : Q);
+    __shared__ uint64_t s[CT * S];                     // operands a | b, then the products
+    uint32_t* sw = reinterpret_cast<uint32_t*>(s);     // the same, as 32-bit words
+    const uint32_t tid = threadIdx.x;
+    for (uint64_t base = (uint64_t)blockIdx.x * CT; base < n; base += (uint64_t)gridDim.x * CT) {
+        const uint32_t rows = (uint32_t)(n - base < CT ? n - base : CT);
+        uint64_t x[M], y[M];
+        if constexpr (sizeof(T) == 8) {
+            const T* ga = a + base * M;
+            const T* gb = b + base * M;
+            for (uint32_t k = tid; k < rows * M; k += CT) {
+                const uint32_t row = k / M, col = k - row * M;
+                s[row * P + col] = ga[k];
+                s[CT * P + row * P + col] = gb[k];
+            }
+            __syncthreads();
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                x[i] = s[tid * P + i];
+                y[i] = s[CT * P + tid * P + i];
+            }
+        } else {
+            constexpr uint32_t BOFF = CT * 2 * M;      // word offset of the b tile (m <= 2M words a row)
+            const T* ga = a + base * m;
+            const T* gb = b + base * m;
+            for (uint32_t k = tid; k < rows * m; k += CT) {
+                sw[k] = ga[k];
+                sw[BOFF + k] = gb[k];
+            }
+            __syncthreads();
+            const uint32_t* ra = sw + tid * m;
+            const uint32_t* rb = sw + BOFF + tid * m;
+#pragma unroll
+            for (int i = 0; i < M; ++i) {
+                const bool hi = i < M - 1 || 2 * M == m;   // word 2i + 1 exists
+                x[i] = ra[2 * i] | (hi ? (uint64_t)ra[2 * i + 1] << 32 : 0ull);
+                y[i] = rb[2 * i] | (hi ? (uint64_t)rb[2 * i + 1] << 32 : 0ull);
+            }
+        }
+        __syncthreads();
+        if constexpr (sizeof(T) == 8) {
+            mul_thread_product<M>(x, y, [&](int c, uint64_t v) { s[tid * Q + c] = v; });
+            __syncthreads();
+            T* gr = r + base * (2 * M);
+            for (uint32_t k = tid; k < rows * 2 * M; k += CT) {
+                const uint32_t row = k / (2 * M), col = k - row * (2 * M);
+                gr[k] = s[row * Q + col];
+            }
+        } else {
+            const uint32_t ow = 2 * m;                 // product words
+            uint32_t* rw = sw + tid * ow;
+            mul_thread_product<M>(x, y, [&](int c, uint64_t v) {
+                if (2u * c < ow) rw[2 * c] = (uint32_t)v;
+                if (2u * c + 1 < ow) rw[2 * c + 1] = (uint32_t)(v >> 32);
+            });
+            __syncthreads();
+            T* gr = r + base * ow;
+            for (uint32_t k = tid; k < rows * ow; k += CT) gr[k] = sw[k];
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T, int M>
+static bi_status mul_thread_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
+    constexpr uint32_t CT = mul_thread_cta<M>();
+    static const int occ = [] {
+        int o = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, mul_thread_kernel<T, M>, CT, 0);
+        return o > 0 ? o : 1;
+    }();
+    const uint64_t tiles = (n + CT - 1) / CT;
+    const uint64_t cap = (uint64_t)num_sms() * (uint64_t)occ;
+    mul_thread_kernel<T, M><<<(unsigned)(tiles < cap ? tiles : cap), CT, 0, st>>>(a, b, r, n, m);
+    return check_launch("mulfull thread kernel");
+}
+
+// Full products of at most MUL_THREAD_MAX_L 64-bit limbs, one thread each.
+template <typename T>
+static bi_status mul_thread(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
+    if constexpr (sizeof(T) == 4) {
+        // an even word count on 8-byte-aligned buffers: the same bytes as m/2 64-bit limbs
+        if (m % 2 == 0 && ((uintptr_t)a | (uintptr_t)b | (uintptr_t)r) % 8 == 0)
+            return mul_thread<uint64_t>(reinterpret_cast<const uint64_t*>(a), reinterpret_cast<const uint64_t*>(b),
+                                        reinterpret_cast<uint64_t*>(r), m / 2, n, st);
+    }
+    switch (sizeof(T) == 8 ? m : (m + 1) / 2) {
+        case 1: return mul_thread_launch<T, 1>(a, b, r, m, n, st);
+        case 2: return mul_thread_launch<T, 2>(a, b, r, m, n, st);
+        case 3: return mul_thread_launch<T, 3>(a, b, r, m, n, st);
+        case 4: return mul_thread_launch<T, 4>(a, b, r, m, n, st);
+        case 5: return mul_thread_launch<T, 5>(a, b, r, m, n, st);
+        case 6: return mul_thread_launch<T, 6>(a, b, r, m, n, st);
+        case 7: return mul_thread_launch<T, 7>(a, b, r, m, n, st);
+        case 8: return mul_thread_launch<T, 8>(a, b, r, m, n, st);
+        case 9: return mul_thread_launch<T, 9>(a, b, r, m, n, st);
+        case 10: return mul_thread_launch<T, 10>(a, b, r, m, n, st);
+        case 11: return mul_thread_launch<T, 11>(a, b, r, m, n, st);
+        case 12: return mul_thread_launch<T, 12>(a, b, r, m, n, st);
+        case 13: return mul_thread_launch<T, 13>(a, b, r, m, n, st);
+        case 14: return mul_thread_launch<T, 14>(a, b, r, m, n, st);
+        case 15: return mul_thread_launch<T, 15>(a, b, r, m, n, st);
+        case 16: return mul_thread_launch<T, 16>(a, b, r, m, n, st);
+        case 17: return mul_thread_launch<T, 17>(a, b, r, m, n, st);
+        case 18: return mul_thread_launch<T, 18>(a, b, r, m, n, st);
+        case 19: return mul_thread_launch<T, 19>(a, b, r, m, n, st);
+        case 20: return mul_thread_launch<T, 20>(a, b, r, m, n, st);
+        case 21: return mul_thread_launch<T, 21>(a, b, r, m, n, st);
+        case 22: return mul_thread_launch<T, 22>(a, b, r, m, n, st);
+        case 23: return mul_thread_launch<T, 23>(a, b, r, m, n, st);
+        case 24: return mul_thread_launch<T, 24>(a, b, r, m, n, st);
+        default: return set_error(BI_EUNSUPPORTED, "mulfull thread kernel: m=%u above its size", m);
+    }
+}
+
+// ---------------------------------------------------------------------------
 
 constexpr uint32_t MUL_MAX_L = 4096;   // u64-view limbs per operand
-constexpr uint32_t MUL_WARP_MAX_L = 32;    // full products up to here take the warp kernel
+constexpr uint32_t MUL_WARP_MAX_L = 32;    // full products above MUL_THREAD_MAX_L up to here: the warp kernel
 
 // ---------------------------------------------------------------------------
 // Tiling of the CTA multiply: instances per CTA (ipc) and row slices per
@@ -294,9 +430,13 @@ template <typename T, bool FULL>
 static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
-    if (FULL && L <= MUL_WARP_MAX_L) {   // the warp kernel unless a tiling of the CTA kernel was tuned for m
+    if (FULL && L <= MUL_WARP_MAX_L) {
+        // the thread kernel (L <= MUL_THREAD_MAX_L) or the warp kernel, unless
+        // a tuning picked one of them ({0, 1}, {0, 0}) or a CTA tiling
         MulTune t;
-        if (!mul_tuning_lookup((int)sizeof(T), FULL, L, &t) || t.ipc == 0) return mul_warp<T>(a, b, r, m, n, st);
+        const bool tuned = mul_tuning_lookup((int)sizeof(T), FULL, L, &t);
+        if (!tuned) return L <= MUL_THREAD_MAX_L ? mul_thread<T>(a, b, r, m, n, st) : mul_warp<T>(a, b, r, m, n, st);
+        if (t.ipc == 0) return t.S == 1 ? mul_thread<T>(a, b, r, m, n, st) : mul_warp<T>(a, b, r, m, n, st);
     }
     return mul_launch_geom<T, FULL>(a, b, r, m, n, mul_geom_for<T, FULL>(L, n), st);
 }
@@ -342,8 +482,10 @@ static bi_status mul_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n,
 // caller's operands, median of `reps` runs each, and record the fastest.
 // For full products of at most MUL_WARP_MAX_L 64-bit limbs the warp kernel
 // (32-bit words: mad.lo/madc.hi column sums) is a candidate too, recorded as
-// ipc = 0, beside the CTA kernel's tilings (64-bit limbs: row_mac8) -- the
-// arithmetic's word width is part of what is tuned.
+// {0, 0}, and for at most MUL_THREAD_MAX_L limbs the thread kernel (64-bit
+// limbs, one thread an instance), recorded as {0, 1}, beside the CTA
+// kernel's tilings (64-bit limbs: row_mac8) -- the arithmetic's word width
+// and the threads an instance are part of what is tuned.
 template <typename T, bool FULL>
 static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t n, int reps, int* chosen,
                               cudaStream_t st) {
@@ -352,15 +494,16 @@ static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t
     const bool warp_ok = FULL && L <= MUL_WARP_MAX_L;
     std::vector<std::pair<uint32_t, uint32_t>> cands;
     if (warp_ok) cands.push_back({0, 0});
+    if (warp_ok && L <= MUL_THREAD_MAX_L) cands.push_back({0, 1});
     for (uint32_t ipc = 1; ipc <= 64; ipc *= 2)
         for (uint32_t S = 1; S <= 4; S *= 2) {
             MulGeom g;
             if (mul_geom_tiled(L, FULL, ipc, S, &g) && (uint64_t)ipc <= n) cands.push_back({ipc, S});
         }
     if (cands.empty()) return set_error(BI_EUNSUPPORTED, "mul autotune: no tiling fits m=%u", m);
-    // one run of a candidate: the warp kernel (ipc = 0) or a CTA tiling
+    // one run of a candidate: the warp kernel {0, 0}, the thread kernel {0, 1} or a CTA tiling
     auto run = [&](uint32_t ipc, uint32_t S) -> bi_status {
-        if (ipc == 0) return mul_warp<T>(a, b, r, m, n, st);
+        if (ipc == 0) return S == 1 ? mul_thread<T>(a, b, r, m, n, st) : mul_warp<T>(a, b, r, m, n, st);
         MulGeom g;
         mul_geom_tiled(L, FULL, ipc, S, &g);
         return mul_launch_geom<T, FULL>(a, b, r, m, n, g, st);
@@ -369,7 +512,7 @@ static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
         return set_error(BI_ECUDA, "mul autotune: %s", cudaGetErrorString(cudaGetLastError()));
     float best = 1e30f;
-    MulTune pick = cands[0].first == 0 ? MulTune{0, 0} : MulTune{cands[0].first, cands[0].second};
+    MulTune pick = {cands[0].first, cands[0].second};
     bi_status st_out = BI_OK;
     for (const auto& c : cands) {
         std::vector<float> ts;
@@ -434,6 +577,13 @@ static bi_status mul_set_tuning(int limb_bytes, uint32_t m, int full, int ipc, i
     if (ipc == 0) {                                   // back to the library's own choice
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune.erase(key);
+        return BI_OK;
+    }
+    if (ipc == -1) {                                  // a per-instance kernel: slices 0 warp, 1 thread
+        if (!full || L > MUL_WARP_MAX_L || slices < 0 || slices > 1 || (slices == 1 && L > MUL_THREAD_MAX_L))
+            return set_error(BI_EINVAL, "mul tuning: no per-instance kernel %d for m=%u (full=%d)", slices, m, full);
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = {0u, (uint32_t)slices};
         return BI_OK;
     }
     MulGeom g;

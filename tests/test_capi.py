@@ -74,7 +74,11 @@ def test_mul_tuning_arguments_checked_on_host(L):
     assert L.bi_mul_set_tuning_u64(0, 1, 4, 1) == 1                  # m == 0
     assert L.bi_mul_set_tuning_u64(64, 1, 4, 3) == 1                 # slices not a power of two
     assert L.bi_mul_set_tuning_u64(64, 1, 4096, 1) == 1              # more instances than a CTA holds
-    assert L.bi_mul_set_tuning_u64(64, 1, -1, 1) == 1
+    assert L.bi_mul_set_tuning_u64(64, 1, -1, 1) == 1                # no per-instance kernel at 64 limbs
+    assert L.bi_mul_set_tuning_u64(25, 1, -1, 1) == 1                # thread kernel: at most 24 limbs
+    assert L.bi_mul_set_tuning_u64(8, 1, -1, 2) == 1                 # no such per-instance kernel
+    assert L.bi_mul_set_tuning_u64(8, 0, -1, 1) == 1                 # truncated products: CTA kernel only
+    assert L.bi_mul_set_tuning_u64(8, 1, -2, 1) == 1
     assert L.bi_mul_set_tuning_u64(1 << 20, 1, 1, 1) == 6            # unsupported size
     fake = ctypes.c_void_p(0x1000)
     assert L.bi_mul_autotune_u64(fake, fake, fake, 64, 0, 1, 3, None, None) == 1   # n == 0
