@@ -375,6 +375,7 @@ def measure_extra(B, L, stream, args):
     sp = int(stream.cuda_stream)
     rates = B.probe_intpipe()
     peak_wps = max(rates.values())
+    peak_gbs = measured_peaks()[0]
     out = {"intpipe_peak_word_products_per_s": peak_wps,
            "intpipe_peak_form": max(rates, key=rates.get)}
     mul = {}
@@ -450,7 +451,9 @@ def measure_extra(B, L, stream, args):
         del a, b, r
     out["mulfull_u64_small"] = small
     div = {}
-    for mv, n in [(4, 1 << 16), (16, 1 << 14), (64, 1 << 13), (256, 1 << 12), (1024, 1 << 10)]:
+    # 2^23 dividend limbs a size: dividends, divisors, quotients and remainders (192 MB) pass
+    # the 129 MB L2, so the small sizes are timed on memory, not on one ~10 us launch
+    for mv, n in [(4, 1 << 20), (16, 1 << 18), (64, 1 << 16), (256, 1 << 14), (1024, 1 << 12)]:
         u = device_uniform_u64(11, n, 2 * mv)
         v = device_uniform_u64(12, n, mv)
         v[:, -1] |= 1
@@ -480,9 +483,12 @@ def measure_extra(B, L, stream, args):
             cpu = {"instances_per_s": round(cpu_sample_rate(lambda: O.div_ref(hu, hv, nthreads=th), k)),
                    "threads": th, "sample": f"the first {k} pairs", "kind": "port",
                    "what": "the oracle's restatement of prototypes/div.c div_shinv (u32 digits), all host threads"}
+        # bytes a division moves: u and v read, q (as many limbs as u), r and a status byte written
+        by = n * (2 * (2 * mv) * 8 + 2 * mv * 8 + 1)
         entry = {"method": method, "instances_per_s": round(n / ms * 1e3), "ms": round(ms, 4), "cpu": cpu,
                  "word_products_per_div": wp, "word_products_per_s": wp * n / ms * 1e3,
                  "frac_of_intpipe_peak": round(wp * n / ms * 1e3 / peak_wps, 4),
+                 "GBps": round(by / ms / 1e6), "frac_of_hbm_peak": round(by / ms * 1e3 / (peak_gbs * 1e9), 4),
                  "shinv_instances_per_s": round(n / ms_shinv * 1e3)}
         if not args.no_cpu:
             # the reference's own work figure: the word products of div.c's multiplications on this
@@ -889,8 +895,9 @@ def summary(extra, achieved_gbs: float, peak_gbs: float):
                                            v["truncated_instances_per_s"]] for k, v in mu.items()}
     sm["mulfull_u64_fields"] = "m: [full inst/s, full frac of int-pipe peak, truncated inst/s]"
     dv = extra.get("div_u64_2m_by_m", {})
-    sm["div_u64_2m_by_m"] = {k.split("_")[0]: [v["instances_per_s"], v["frac_of_intpipe_peak"]] for k, v in dv.items()}
-    sm["div_fields"] = "m: [div/s, frac of int-pipe peak in the method's own limb products]"
+    sm["div_u64_2m_by_m"] = {k.split("_")[0]: [v["instances_per_s"], v["frac_of_intpipe_peak"], v["frac_of_hbm_peak"]]
+                             for k, v in dv.items()}
+    sm["div_fields"] = "m: [div/s, frac of int-pipe peak in the method's own limb products, frac of HBM peak]"
     if "mul2048_u32" in extra:
         sm["c1_mulfull_u32_2048bit_inst_per_s"] = extra["mul2048_u32"]["instances_per_s"]
     ub = extra.get("uneven_batch")
