@@ -435,6 +435,10 @@ def measure_extra(B, L, stream, args):
         r = torch.empty((n, 2 * m), dtype=torch.int64, device="cuda")
         ms = graph_time(lambda st: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, st)), 5)
         wp = n * (2 * m) ** 2
+        # the truncated product (mod B^m, the reference's convMul semantics): m(m+1)/2 limb products
+        rt = torch.empty((n, m), dtype=torch.int64, device="cuda")
+        ms_t = graph_time(lambda st: check(L, L.bi_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, st)), 5)
+        wp_t = n * 4 * m * (m + 1) // 2
         # the autotuner weighs the thread and warp kernels against the CTA tilings (64-bit limbs)
         chosen = (ctypes.c_int * 2)()
         check(L, L.bi_mul_autotune_u64(a.data_ptr(), b.data_ptr(), r.data_ptr(), m, n, 1, 3,
@@ -447,8 +451,10 @@ def measure_extra(B, L, stream, args):
                 f"CTA kernel, 64-bit limbs, {chosen[0]} instances x {chosen[1]} slices")
         small[f"m{m}_n{n}"] = {"instances_per_s": round(n / ms * 1e3), "word_products_per_s": wp / ms * 1e3,
                                "frac_of_intpipe_peak": round(wp / ms * 1e3 / peak_wps, 4),
+                               "truncated_instances_per_s": round(n / ms_t * 1e3),
+                               "truncated_frac_of_intpipe_peak": round(wp_t / ms_t * 1e3 / peak_wps, 4),
                                "autotuned_instances_per_s": round(n / ms_tuned * 1e3), "autotuned_pick": pick}
-        del a, b, r
+        del a, b, r, rt
     out["mulfull_u64_small"] = small
     div = {}
     # 2^23 dividend limbs a size: dividends, divisors, quotients and remainders (192 MB) pass

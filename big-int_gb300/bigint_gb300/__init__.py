@@ -290,7 +290,7 @@ def div(u, v, q=None, r=None, status=None, stream=None, method="auto"):
 def mul_autotune(a, b, r=None, full: bool = True, reps: int = 3, stream=None):
     """Time the CTA multiply's tilings on (a, b) -- and the 32-bit-word warp
     kernel for full products of at most 32 64-bit limbs, the one-thread-an-
-    instance kernel for at most 24 -- and keep the fastest for this (limb
+    instance kernel for products of at most 24 -- and keep the fastest for this (limb
     width, full, m); returns (instances per CTA, slices), (0, 0) when the warp
     kernel was fastest, (0, 1) for the thread kernel.  r receives the product
     as mulfull/mul write it."""
@@ -309,8 +309,8 @@ def mul_autotune(a, b, r=None, full: bool = True, reps: int = 3, stream=None):
 
 def mul_set_tuning(m: int, dtype, full: bool, ipc: int, slices: int = 1):
     """Set the CTA multiply's tiling for (limb width, full, m) by hand; ipc=-1
-    picks a per-instance kernel for a full product (slices 0: the warp kernel,
-    1: the thread kernel); ipc=0 returns to the library's own choice."""
+    picks a per-instance kernel (slices 0: the warp kernel, full products
+    only; 1: the thread kernel); ipc=0 returns to the library's own choice."""
     w = "u64" if np.dtype(dtype).itemsize == 8 else "u32"
     _check(getattr(lib(), f"bi_mul_set_tuning_{w}")(m, 1 if full else 0, ipc, slices))
 

@@ -213,9 +213,9 @@ static bi_status mul_warp(const T* a, const T* b, T* r, uint32_t m, uint64_t n, 
 }
 
 // ---------------------------------------------------------------------------
-// One thread per instance for full products of at most MUL_THREAD_MAX_L
-// 64-bit limbs (multhread.cuh): the library's default there, for both limb
-// types.  A CTA moves mul_thread_cta<M>() instances' operands into shared memory
+// One thread per instance for products (full or truncated) of at most
+// MUL_THREAD_MAX_L 64-bit limbs (multhread.cuh): the library's default
+// there, for both limb types.  A CTA moves mul_thread_cta<M>() instances' operands into shared memory
 // with coalesced loads, each thread multiplies its own row in registers and
 // leaves the product in shared memory, and the CTA writes the tile back with
 // coalesced stores.  64-bit limbs (u64, and u32 batches of an even word count
@@ -225,12 +225,13 @@ static bi_status mul_warp(const T* a, const T* b, T* r, uint32_t m, uint64_t n, 
 // kept as the words arrive (row stride m, odd, so each thread's 32-bit reads
 // are conflict-free too) and the product at stride 2m words.
 // ---------------------------------------------------------------------------
-template <typename T, int M>
+template <typename T, int M, bool FULL>
 __global__ void __launch_bounds__(mul_thread_cta<M>())
 mul_thread_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restrict__ r, uint64_t n, uint32_t m) {
     constexpr uint32_t CT = mul_thread_cta<M>();
     constexpr uint32_t P = (M % 2 == 0) ? M + 1 : M;    // operand row stride (limbs)
-    constexpr uint32_t Q = 2 * M + 1;                  // product row stride (limbs)
+    constexpr uint32_t OL = FULL ? 2 * M : M;          // product limbs
+    constexpr uint32_t Q = FULL ? 2 * M + 1 : P;       // product row stride (limbs)
     constexpr uint32_t S = (2 * P > Q ? 2 * P : Q);
     __shared__ uint64_t s[CT * S];                     // operands a | b, then the products
     uint32_t* sw = reinterpret_cast<uint32_t*>(s);     // the same, as 32-bit words
@@ -272,17 +273,17 @@ mul_thread_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restric
         }
         __syncthreads();
         if constexpr (sizeof(T) == 8) {
-            mul_thread_product<M>(x, y, [&](int c, uint64_t v) { s[tid * Q + c] = v; });
+            mul_thread_product<M, FULL>(x, y, [&](int c, uint64_t v) { s[tid * Q + c] = v; });
             __syncthreads();
-            T* gr = r + base * (2 * M);
-            for (uint32_t k = tid; k < rows * 2 * M; k += CT) {
-                const uint32_t row = k / (2 * M), col = k - row * (2 * M);
+            T* gr = r + base * OL;
+            for (uint32_t k = tid; k < rows * OL; k += CT) {
+                const uint32_t row = k / OL, col = k - row * OL;
                 gr[k] = s[row * Q + col];
             }
         } else {
-            const uint32_t ow = 2 * m;                 // product words
+            const uint32_t ow = FULL ? 2 * m : m;      // product words
             uint32_t* rw = sw + tid * ow;
-            mul_thread_product<M>(x, y, [&](int c, uint64_t v) {
+            mul_thread_product<M, FULL>(x, y, [&](int c, uint64_t v) {
                 if (2u * c < ow) rw[2 * c] = (uint32_t)v;
                 if (2u * c + 1 < ow) rw[2 * c + 1] = (uint32_t)(v >> 32);
             });
@@ -294,55 +295,55 @@ mul_thread_kernel(const T* __restrict__ a, const T* __restrict__ b, T* __restric
     }
 }
 
-template <typename T, int M>
+template <typename T, int M, bool FULL>
 static bi_status mul_thread_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     constexpr uint32_t CT = mul_thread_cta<M>();
     static const int occ = [] {
         int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, mul_thread_kernel<T, M>, CT, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, mul_thread_kernel<T, M, FULL>, CT, 0);
         return o > 0 ? o : 1;
     }();
     const uint64_t tiles = (n + CT - 1) / CT;
     const uint64_t cap = (uint64_t)num_sms() * (uint64_t)occ;
-    mul_thread_kernel<T, M><<<(unsigned)(tiles < cap ? tiles : cap), CT, 0, st>>>(a, b, r, n, m);
-    return check_launch("mulfull thread kernel");
+    mul_thread_kernel<T, M, FULL><<<(unsigned)(tiles < cap ? tiles : cap), CT, 0, st>>>(a, b, r, n, m);
+    return check_launch(FULL ? "mulfull thread kernel" : "mul thread kernel");
 }
 
-// Full products of at most MUL_THREAD_MAX_L 64-bit limbs, one thread each.
-template <typename T>
+// Products of at most MUL_THREAD_MAX_L 64-bit limbs, one thread each.
+template <typename T, bool FULL>
 static bi_status mul_thread(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     if constexpr (sizeof(T) == 4) {
         // an even word count on 8-byte-aligned buffers: the same bytes as m/2 64-bit limbs
         if (m % 2 == 0 && ((uintptr_t)a | (uintptr_t)b | (uintptr_t)r) % 8 == 0)
-            return mul_thread<uint64_t>(reinterpret_cast<const uint64_t*>(a), reinterpret_cast<const uint64_t*>(b),
+            return mul_thread<uint64_t, FULL>(reinterpret_cast<const uint64_t*>(a), reinterpret_cast<const uint64_t*>(b),
                                         reinterpret_cast<uint64_t*>(r), m / 2, n, st);
     }
     switch (sizeof(T) == 8 ? m : (m + 1) / 2) {
-        case 1: return mul_thread_launch<T, 1>(a, b, r, m, n, st);
-        case 2: return mul_thread_launch<T, 2>(a, b, r, m, n, st);
-        case 3: return mul_thread_launch<T, 3>(a, b, r, m, n, st);
-        case 4: return mul_thread_launch<T, 4>(a, b, r, m, n, st);
-        case 5: return mul_thread_launch<T, 5>(a, b, r, m, n, st);
-        case 6: return mul_thread_launch<T, 6>(a, b, r, m, n, st);
-        case 7: return mul_thread_launch<T, 7>(a, b, r, m, n, st);
-        case 8: return mul_thread_launch<T, 8>(a, b, r, m, n, st);
-        case 9: return mul_thread_launch<T, 9>(a, b, r, m, n, st);
-        case 10: return mul_thread_launch<T, 10>(a, b, r, m, n, st);
-        case 11: return mul_thread_launch<T, 11>(a, b, r, m, n, st);
-        case 12: return mul_thread_launch<T, 12>(a, b, r, m, n, st);
-        case 13: return mul_thread_launch<T, 13>(a, b, r, m, n, st);
-        case 14: return mul_thread_launch<T, 14>(a, b, r, m, n, st);
-        case 15: return mul_thread_launch<T, 15>(a, b, r, m, n, st);
-        case 16: return mul_thread_launch<T, 16>(a, b, r, m, n, st);
-        case 17: return mul_thread_launch<T, 17>(a, b, r, m, n, st);
-        case 18: return mul_thread_launch<T, 18>(a, b, r, m, n, st);
-        case 19: return mul_thread_launch<T, 19>(a, b, r, m, n, st);
-        case 20: return mul_thread_launch<T, 20>(a, b, r, m, n, st);
-        case 21: return mul_thread_launch<T, 21>(a, b, r, m, n, st);
-        case 22: return mul_thread_launch<T, 22>(a, b, r, m, n, st);
-        case 23: return mul_thread_launch<T, 23>(a, b, r, m, n, st);
-        case 24: return mul_thread_launch<T, 24>(a, b, r, m, n, st);
-        default: return set_error(BI_EUNSUPPORTED, "mulfull thread kernel: m=%u above its size", m);
+        case 1: return mul_thread_launch<T, 1, FULL>(a, b, r, m, n, st);
+        case 2: return mul_thread_launch<T, 2, FULL>(a, b, r, m, n, st);
+        case 3: return mul_thread_launch<T, 3, FULL>(a, b, r, m, n, st);
+        case 4: return mul_thread_launch<T, 4, FULL>(a, b, r, m, n, st);
+        case 5: return mul_thread_launch<T, 5, FULL>(a, b, r, m, n, st);
+        case 6: return mul_thread_launch<T, 6, FULL>(a, b, r, m, n, st);
+        case 7: return mul_thread_launch<T, 7, FULL>(a, b, r, m, n, st);
+        case 8: return mul_thread_launch<T, 8, FULL>(a, b, r, m, n, st);
+        case 9: return mul_thread_launch<T, 9, FULL>(a, b, r, m, n, st);
+        case 10: return mul_thread_launch<T, 10, FULL>(a, b, r, m, n, st);
+        case 11: return mul_thread_launch<T, 11, FULL>(a, b, r, m, n, st);
+        case 12: return mul_thread_launch<T, 12, FULL>(a, b, r, m, n, st);
+        case 13: return mul_thread_launch<T, 13, FULL>(a, b, r, m, n, st);
+        case 14: return mul_thread_launch<T, 14, FULL>(a, b, r, m, n, st);
+        case 15: return mul_thread_launch<T, 15, FULL>(a, b, r, m, n, st);
+        case 16: return mul_thread_launch<T, 16, FULL>(a, b, r, m, n, st);
+        case 17: return mul_thread_launch<T, 17, FULL>(a, b, r, m, n, st);
+        case 18: return mul_thread_launch<T, 18, FULL>(a, b, r, m, n, st);
+        case 19: return mul_thread_launch<T, 19, FULL>(a, b, r, m, n, st);
+        case 20: return mul_thread_launch<T, 20, FULL>(a, b, r, m, n, st);
+        case 21: return mul_thread_launch<T, 21, FULL>(a, b, r, m, n, st);
+        case 22: return mul_thread_launch<T, 22, FULL>(a, b, r, m, n, st);
+        case 23: return mul_thread_launch<T, 23, FULL>(a, b, r, m, n, st);
+        case 24: return mul_thread_launch<T, 24, FULL>(a, b, r, m, n, st);
+        default: return set_error(BI_EUNSUPPORTED, "mul thread kernel: m=%u above its size", m);
     }
 }
 
@@ -430,13 +431,17 @@ template <typename T, bool FULL>
 static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
-    if (FULL && L <= MUL_WARP_MAX_L) {
-        // the thread kernel (L <= MUL_THREAD_MAX_L) or the warp kernel, unless
-        // a tuning picked one of them ({0, 1}, {0, 0}) or a CTA tiling
+    if (L <= MUL_THREAD_MAX_L || (FULL && L <= MUL_WARP_MAX_L)) {
+        // the thread kernel (L <= MUL_THREAD_MAX_L) or, for full products, the
+        // warp kernel, unless a tuning picked one of them ({0, 1}, {0, 0}) or
+        // a CTA tiling
         MulTune t;
         const bool tuned = mul_tuning_lookup((int)sizeof(T), FULL, L, &t);
-        if (!tuned) return L <= MUL_THREAD_MAX_L ? mul_thread<T>(a, b, r, m, n, st) : mul_warp<T>(a, b, r, m, n, st);
-        if (t.ipc == 0) return t.S == 1 ? mul_thread<T>(a, b, r, m, n, st) : mul_warp<T>(a, b, r, m, n, st);
+        if (!tuned || t.ipc == 0) {
+            const bool thread = tuned ? t.S == 1 : L <= MUL_THREAD_MAX_L;
+            if (thread) return mul_thread<T, FULL>(a, b, r, m, n, st);
+            if constexpr (FULL) return mul_warp<T>(a, b, r, m, n, st);
+        }
     }
     return mul_launch_geom<T, FULL>(a, b, r, m, n, mul_geom_for<T, FULL>(L, n), st);
 }
@@ -482,8 +487,9 @@ static bi_status mul_chain(const T* a, const T* b, T* r, uint32_t m, uint64_t n,
 // caller's operands, median of `reps` runs each, and record the fastest.
 // For full products of at most MUL_WARP_MAX_L 64-bit limbs the warp kernel
 // (32-bit words: mad.lo/madc.hi column sums) is a candidate too, recorded as
-// {0, 0}, and for at most MUL_THREAD_MAX_L limbs the thread kernel (64-bit
-// limbs, one thread an instance), recorded as {0, 1}, beside the CTA
+// {0, 0}, and for products (full or truncated) of at most MUL_THREAD_MAX_L
+// limbs the thread kernel (64-bit limbs, one thread an instance), recorded
+// as {0, 1}, beside the CTA
 // kernel's tilings (64-bit limbs: row_mac8) -- the arithmetic's word width
 // and the threads an instance are part of what is tuned.
 template <typename T, bool FULL>
@@ -494,7 +500,7 @@ static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t
     const bool warp_ok = FULL && L <= MUL_WARP_MAX_L;
     std::vector<std::pair<uint32_t, uint32_t>> cands;
     if (warp_ok) cands.push_back({0, 0});
-    if (warp_ok && L <= MUL_THREAD_MAX_L) cands.push_back({0, 1});
+    if (L <= MUL_THREAD_MAX_L) cands.push_back({0, 1});
     for (uint32_t ipc = 1; ipc <= 64; ipc *= 2)
         for (uint32_t S = 1; S <= 4; S *= 2) {
             MulGeom g;
@@ -503,7 +509,11 @@ static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t
     if (cands.empty()) return set_error(BI_EUNSUPPORTED, "mul autotune: no tiling fits m=%u", m);
     // one run of a candidate: the warp kernel {0, 0}, the thread kernel {0, 1} or a CTA tiling
     auto run = [&](uint32_t ipc, uint32_t S) -> bi_status {
-        if (ipc == 0) return S == 1 ? mul_thread<T>(a, b, r, m, n, st) : mul_warp<T>(a, b, r, m, n, st);
+        if (ipc == 0) {
+            if (S == 1) return mul_thread<T, FULL>(a, b, r, m, n, st);
+            if constexpr (FULL) return mul_warp<T>(a, b, r, m, n, st);
+            return set_error(BI_EINVAL, "mul autotune: no warp kernel for truncated products");
+        }
         MulGeom g;
         mul_geom_tiled(L, FULL, ipc, S, &g);
         return mul_launch_geom<T, FULL>(a, b, r, m, n, g, st);
@@ -580,8 +590,8 @@ static bi_status mul_set_tuning(int limb_bytes, uint32_t m, int full, int ipc, i
         return BI_OK;
     }
     if (ipc == -1) {                                  // a per-instance kernel: slices 0 warp, 1 thread
-        if (!full || L > MUL_WARP_MAX_L || slices < 0 || slices > 1 || (slices == 1 && L > MUL_THREAD_MAX_L))
-            return set_error(BI_EINVAL, "mul tuning: no per-instance kernel %d for m=%u (full=%d)", slices, m, full);
+        const bool ok = (slices == 0 && full && L <= MUL_WARP_MAX_L) || (slices == 1 && L <= MUL_THREAD_MAX_L);
+        if (!ok) return set_error(BI_EINVAL, "mul tuning: no per-instance kernel %d for m=%u (full=%d)", slices, m, full);
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[key] = {0u, (uint32_t)slices};
         return BI_OK;

@@ -1,8 +1,8 @@
-// multhread.cuh -- full products of at most 24 64-bit limbs, one thread per
-// instance.
+// multhread.cuh -- products (full or truncated) of at most 24 64-bit limbs,
+// one thread per instance.
 //
 // A thread holds both operands in registers (M 64-bit limbs each, M a
-// compile-time size) and forms the 2M-limb product column by column
+// compile-time size) and forms the product (2M limbs, or the low M) column by column
 // (product scanning, Comba's method): column c adds a_i * b_{c-i} for every
 // i into a three-limb accumulator -- one mul.lo/mul.hi pair and an
 // add/addc/addc chain a term -- emits the low limb and shifts the
@@ -34,15 +34,18 @@ __device__ __forceinline__ void mac3(uint64_t& c0, uint64_t& c1, uint32_t& c2, u
         : "l"(x), "l"(y));
 }
 
-// The full product of x and y (M limbs each); put(c, limb) receives limbs
-// 0 .. 2M-1 in order.  A column holds at most M terms below 2^128, so with
-// the carry from the column below the accumulator stays below 2^160.
-template <int M, typename Put>
+// The product of x and y (M limbs each): the full 2M limbs (FULL), or the
+// low M (the product mod B^M: only the columns below M are formed, about
+// half the terms); put(c, limb) receives the limbs in order.  A column holds
+// at most M terms below 2^128, so with the carry from the column below the
+// accumulator stays below 2^160.
+template <int M, bool FULL, typename Put>
 __device__ __forceinline__ void mul_thread_product(const uint64_t (&x)[M], const uint64_t (&y)[M], Put put) {
+    constexpr int COLS = FULL ? 2 * M - 1 : M;
     uint64_t c0 = 0, c1 = 0;
     uint32_t c2 = 0;
 #pragma unroll
-    for (int c = 0; c < 2 * M - 1; ++c) {
+    for (int c = 0; c < COLS; ++c) {
 #pragma unroll
         for (int i = (c - M + 1 > 0 ? c - M + 1 : 0); i <= (c < M - 1 ? c : M - 1); ++i)
             mac3(c0, c1, c2, x[i], y[c - i]);
@@ -51,7 +54,7 @@ __device__ __forceinline__ void mul_thread_product(const uint64_t (&x)[M], const
         c1 = c2;
         c2 = 0;
     }
-    put(2 * M - 1, c0);
+    if constexpr (FULL) put(2 * M - 1, c0);
 }
 
 }  // namespace bi

@@ -77,7 +77,7 @@ def test_mul_tuning_arguments_checked_on_host(L):
     assert L.bi_mul_set_tuning_u64(64, 1, -1, 1) == 1                # no per-instance kernel at 64 limbs
     assert L.bi_mul_set_tuning_u64(25, 1, -1, 1) == 1                # thread kernel: at most 24 limbs
     assert L.bi_mul_set_tuning_u64(8, 1, -1, 2) == 1                 # no such per-instance kernel
-    assert L.bi_mul_set_tuning_u64(8, 0, -1, 1) == 1                 # truncated products: CTA kernel only
+    assert L.bi_mul_set_tuning_u64(8, 0, -1, 0) == 1                 # truncated products: no warp kernel
     assert L.bi_mul_set_tuning_u64(8, 1, -2, 1) == 1
     assert L.bi_mul_set_tuning_u64(1 << 20, 1, 1, 1) == 6            # unsupported size
     fake = ctypes.c_void_p(0x1000)

@@ -1,9 +1,10 @@
-"""Full products of at most 32 64-bit limbs on the per-instance kernels: the
-thread kernel (one thread an instance, 64-bit limbs; the default up to 24
-limbs) and the warp kernel (32-bit words; the default from 25 to 32 limbs),
-each pinned by hand at every size it takes, both limb widths, against the
-oracle: saturated columns, zeros, single bits, ragged last tiles, and a batch
-larger than one wave of the thread kernel's grid (the grid-stride loop)."""
+"""Products of at most 32 64-bit limbs on the per-instance kernels: the
+thread kernel (one thread an instance, 64-bit limbs; the default for full
+and truncated products up to 24 limbs) and the warp kernel (32-bit words;
+full products only, the default from 25 to 32 limbs), each pinned by hand at
+every size it takes, both limb widths, against the oracle: saturated
+columns, zeros, single bits, ragged last tiles, and a batch larger than one
+wave of the thread kernel's grid (the grid-stride loop)."""
 import numpy as np
 import pytest
 
@@ -43,29 +44,34 @@ def _reset(bigint):
         for dt in (np.uint64, np.uint32):
             if _limbs64(m, dt) <= WARP_MAX_L:
                 bigint.mul_set_tuning(m, dt, True, 0)
+                bigint.mul_set_tuning(m, dt, False, 0)
 
 
 @pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
-@pytest.mark.parametrize("kernel", ["default", "thread", "warp"])
-def test_every_small_size(bigint, oracle, dtype, kernel):
+@pytest.mark.parametrize("kernel,full", [("default", True), ("thread", True), ("warp", True),
+                                         ("default", False), ("thread", False)])
+def test_every_small_size(bigint, oracle, dtype, kernel, full):
     B = bigint
-    top_m = THREAD_MAX_L if kernel == "thread" else WARP_MAX_L
+    top_m = THREAD_MAX_L if kernel == "thread" or not full else WARP_MAX_L
     sizes = range(1, (top_m if dtype == np.uint64 else 2 * top_m) + 1)
     for m in sizes:
         if kernel != "default":
-            B.mul_set_tuning(m, dtype, True, -1, 1 if kernel == "thread" else 0)
+            B.mul_set_tuning(m, dtype, full, -1, 1 if kernel == "thread" else 0)
         n = 128 + 3 + m                          # one full tile and a ragged one
         a, b = _cases(3000 + m, n, m, dtype)
         da, db = B.to_device(a), B.to_device(b)
-        got = B.to_host(B.mulfull(da, db), dtype)
-        assert (got == oracle.mulfull(a, b)).all(), (m, dtype, kernel)
+        if full:
+            assert (B.to_host(B.mulfull(da, db), dtype) == oracle.mulfull(a, b)).all(), (m, dtype, kernel)
+        else:
+            assert (B.to_host(B.mul(da, db), dtype) == oracle.mul(a, b)).all(), (m, dtype, kernel)
         if kernel != "default":
-            B.mul_set_tuning(m, dtype, True, 0)
+            B.mul_set_tuning(m, dtype, full, 0)
 
 
+@pytest.mark.parametrize("full", [True, False])
 @pytest.mark.parametrize("m,dtype", [(1, np.uint64), (3, np.uint32), (16, np.uint64), (31, np.uint32), (24, np.uint64),
                                      (47, np.uint32)])
-def test_batch_larger_than_the_grid(bigint, m, dtype):
+def test_batch_larger_than_the_grid(bigint, m, dtype, full):
     """More instances than the capped grid holds at once (152 SMs x CTAs an SM
     x 128 or 64 instances): rows in every wave, checked as Python integers."""
     B = bigint
@@ -74,15 +80,17 @@ def test_batch_larger_than_the_grid(bigint, m, dtype):
     b = uniform_limbs(78 + m, n, m, dtype)
     a[-1] = np.iinfo(dtype).max
     b[-1] = np.iinfo(dtype).max
-    got = B.to_host(B.mulfull(B.to_device(a), B.to_device(b)), dtype)
+    da, db = B.to_device(a), B.to_device(b)
+    got = B.to_host(B.mulfull(da, db) if full else B.mul(da, db), dtype)
     w = 8 * a.itemsize
+    mod = 1 << (w * (2 * m if full else m))
 
     def val(row):
         return sum(int(x) << (w * k) for k, x in enumerate(row))
 
     rows = np.unique(np.concatenate([np.arange(0, n, 9973), [n - 129, n - 128, n - 1], np.arange(127, n, 311_296)]))
     for i in rows:
-        assert val(got[i]) == val(a[i]) * val(b[i]), (m, dtype, int(i))
+        assert val(got[i]) == val(a[i]) * val(b[i]) % mod, (m, dtype, int(i))
 
 
 @pytest.mark.parametrize("m", [2, 8, 31, 32, 47, 48])
@@ -108,6 +116,11 @@ def test_u32_buffers_off_an_8_byte_boundary(bigint, oracle, m):
     B.mulfull(da, db, out=r)
     assert (B.to_host(r, np.uint32) == oracle.mulfull(a, b)).all()
     assert int(rbuf[0]) == 0                                  # nothing written before the product
+    tbuf = torch.zeros(n * m + 1, dtype=torch.int32, device="cuda")
+    t = tbuf[1:].view(n, m)
+    B.mul(da, db, out=t)
+    assert (B.to_host(t, np.uint32) == oracle.mul(a, b)).all()
+    assert int(tbuf[0]) == 0
 
 
 def test_pinning_checked(bigint):
@@ -122,6 +135,9 @@ def test_pinning_checked(bigint):
     with pytest.raises(B.BigIntError):
         B.mul_set_tuning(8, np.uint64, True, -1, 2)         # no such kernel
     with pytest.raises(B.BigIntError):
-        B.mul_set_tuning(8, np.uint64, False, -1, 1)        # truncated products: CTA kernel only
+        B.mul_set_tuning(8, np.uint64, False, -1, 0)        # truncated products: no warp kernel
+    with pytest.raises(B.BigIntError):
+        B.mul_set_tuning(25, np.uint64, False, -1, 1)       # thread kernel above 24 limbs
     B.mul_set_tuning(33, np.uint32, True, -1, 0)            # 17 64-bit limbs on the warp kernel: fine
     B.mul_set_tuning(48, np.uint32, True, -1, 1)            # 24 64-bit limbs on the thread kernel: fine
+    B.mul_set_tuning(24, np.uint64, False, -1, 1)           # truncated, on the thread kernel: fine

@@ -13,7 +13,8 @@ pytestmark = pytest.mark.gpu
 def _reset(bigint):
     yield
     for m, dt in ((64, np.uint64), (100, np.uint64), (256, np.uint64), (200, np.uint32), (16, np.uint64),
-                  (2, np.uint64), (4, np.uint64), (32, np.uint64), (40, np.uint32)):
+                  (2, np.uint64), (4, np.uint64), (32, np.uint64), (40, np.uint32), (8, np.uint64),
+                  (24, np.uint64), (33, np.uint32)):
         for full in (False, True):
             bigint.mul_set_tuning(m, dt, full, 0)
 
@@ -78,6 +79,27 @@ def test_autotune_weighs_the_warp_kernel_at_small_sizes(bigint, oracle, m, dtype
     assert (B.to_host(r, dtype) == oracle.mulfull(a, b)).all()
     assert (B.to_host(B.mulfull(da, db), dtype) == oracle.mulfull(a, b)).all()
     B.mul_set_tuning(m, dtype, True, 0)
+
+
+@pytest.mark.parametrize("m,dtype", [(8, np.uint64), (24, np.uint64), (33, np.uint32)])
+def test_autotune_truncated_small_sizes(bigint, oracle, m, dtype):
+    """Truncated products of at most 24 64-bit limbs: the autotuner times the
+    thread kernel (reported as (0, 1)) beside the CTA tilings; r and later
+    calls are exact whichever wins."""
+    import torch
+
+    B = bigint
+    n = 700
+    a = uniform_limbs(921 + m, n, m, dtype)
+    b = uniform_limbs(922 + m, n, m, dtype)
+    a[0] = np.iinfo(dtype).max
+    b[0] = np.iinfo(dtype).max
+    da, db = B.to_device(a), B.to_device(b)
+    r = torch.zeros((n, m), dtype=torch.int64 if dtype == np.uint64 else torch.int32, device="cuda")
+    ipc, slices = B.mul_autotune(da, db, r, full=False, reps=2)
+    assert (ipc, slices) == (0, 1) or (ipc >= 1 and slices in (1, 2, 4))
+    assert (B.to_host(r, dtype) == oracle.mul(a, b)).all()
+    assert (B.to_host(B.mul(da, db), dtype) == oracle.mul(a, b)).all()
 
 
 @pytest.mark.parametrize("m", [4, 16, 32])
