@@ -906,6 +906,10 @@ def summary(extra, achieved_gbs: float, peak_gbs: float):
     sm["div_fields"] = "m: [div/s, frac of int-pipe peak in the method's own limb products, frac of HBM peak]"
     if "mul2048_u32" in extra:
         sm["c1_mulfull_u32_2048bit_inst_per_s"] = extra["mul2048_u32"]["instances_per_s"]
+    sp = extra.get("mulfull_u64_small", {})
+    sm["mul_u64_small"] = {k.split("_")[0]: [v["instances_per_s"], v["frac_of_intpipe_peak"],
+                                             v.get("truncated_instances_per_s")] for k, v in sp.items()}
+    sm["mul_u64_small_fields"] = "m: [full inst/s, full frac of int-pipe peak, truncated inst/s]"
     ub = extra.get("uneven_batch")
     if ub:
         sm["uneven_batch_100k"] = {"inst_per_s": ub["batched_inst_per_s"],
