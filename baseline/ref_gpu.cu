@@ -129,6 +129,8 @@ int ref_add_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, v
 int ref_mul_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     switch (m) {
+    case 16: return launch_mul<U64bits, 16>(a, b, r, n, s);
+    case 32: return launch_mul<U64bits, 32>(a, b, r, n, s);
     case 64: return launch_mul<U64bits, 64>(a, b, r, n, s);
     case 128: return launch_mul<U64bits, 128>(a, b, r, n, s);
     case 256: return launch_mul<U64bits, 256>(a, b, r, n, s);
@@ -142,6 +144,8 @@ int ref_mul_u64(const void* a, const void* b, void* r, uint32_t m, uint32_t n, v
 int ref_mul_u32(const void* a, const void* b, void* r, uint32_t m, uint32_t n, void* stream) {
     cudaStream_t s = (cudaStream_t)stream;
     switch (m) {
+    case 16: return launch_mul<U32bits, 16>(a, b, r, n, s);
+    case 32: return launch_mul<U32bits, 32>(a, b, r, n, s);
     case 64: return launch_mul<U32bits, 64>(a, b, r, n, s);
     case 128: return launch_mul<U32bits, 128>(a, b, r, n, s);
     default: return 1;

@@ -62,8 +62,8 @@ def lib():
 
 
 ADD_SIZES = [16, 32, 64, 128, 256, 512, 1024, 2048, 4096]   # u64 limbs
-MUL_SIZES_U64 = [64, 128, 256, 512, 1024, 2048]
-MUL_SIZES_U32 = [64, 128]
+MUL_SIZES_U64 = [16, 32, 64, 128, 256, 512, 1024, 2048]   # the reference's own sweep reaches 16 (cuda/main.cu:501-512)
+MUL_SIZES_U32 = [16, 32, 64, 128]
 ADD10_SIZES = [16, 128, 1024, 4096]   # u64 limbs (baddKer3Bench<..., 10>)
 ADD10_V1_SIZES = [16, 128, 1024]      # baddKer1Bench<..., 10> (one instance per block, m <= 1024)
 MUL6_SIZES = [64, 256, 1024]          # u64 limbs (convMul5Bench<..., 6>)

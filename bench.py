@@ -736,7 +736,7 @@ def measure_reference_kernels(B, L, stream):
     """The reference's own kernels (baddKer3, convMul5) on the same GPU and inputs."""
     import torch
 
-    from bigint_gb300.workloads import MUL_U64, addsub_u64_device, mul2048_u32, mul_u64_device
+    from bigint_gb300.workloads import MUL_U64, addsub_u64_device, device_uniform_u64, mul2048_u32, mul_u64_device
 
     sys.path.insert(0, os.path.join(REPO, "baseline"))
     try:
@@ -786,6 +786,30 @@ def measure_reference_kernels(B, L, stream):
             entry["full_reference"] = "unavailable: convMul5 at 2m=%d limbs needs >48 KiB static shared memory" % (2 * m)
         res["mul_u64"][f"m{m}_n{n}"] = entry
         del a, b, rt
+    # the small end of the reference's own multiply sweep (cuda/main.cu:511-512), 2^22 limbs an
+    # operand: convMul5 at m (truncated) and at 2m on zero-padded inputs (full), graph-timed as both
+    # are a few microseconds a launch
+    res["mul_u64_small"] = {}
+    for m in (16, 32):
+        n = (1 << 22) // m
+        a = device_uniform_u64(41, n, m)
+        b = device_uniform_u64(42, n, m)
+        rt = torch.empty_like(a)
+        ms_tr = graph_time(lambda st: R.ref_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n, st), 5)
+        ms_ours_tr = graph_time(lambda st: check(L, L.bi_mul_u64(a.data_ptr(), b.data_ptr(), rt.data_ptr(), m, n,
+                                                                 st)), 5)
+        pa = torch.zeros((n, 2 * m), dtype=torch.int64, device="cuda")
+        pb = torch.zeros_like(pa)
+        pa[:, :m] = a
+        pb[:, :m] = b
+        rf = torch.empty_like(pa)
+        ms_f = graph_time(lambda st: R.ref_mul_u64(pa.data_ptr(), pb.data_ptr(), rf.data_ptr(), 2 * m, n, st), 5)
+        ms_ours_f = graph_time(lambda st: check(L, L.bi_mulfull_u64(a.data_ptr(), b.data_ptr(), rf.data_ptr(), m, n,
+                                                                    st)), 5)
+        res["mul_u64_small"][f"m{m}_n{n}"] = {
+            "truncated_reference_inst_per_s": round(n / ms_tr * 1e3), "truncated_ours_inst_per_s": round(n / ms_ours_tr * 1e3),
+            "full_reference_inst_per_s": round(n / ms_f * 1e3), "full_ours_inst_per_s": round(n / ms_ours_f * 1e3)}
+        del a, b, rt, pa, pb, rf
     a, b = mul2048_u32()
     n, m = a.shape
     pa = np.zeros((n, 2 * m), np.uint32)
@@ -926,6 +950,11 @@ def summary(extra, achieved_gbs: float, peak_gbs: float):
             "truncated": round(v["truncated_ours_inst_per_s"] / v["truncated_reference_inst_per_s"], 2),
             "full": (round(v["full_ours_inst_per_s"] / v["full_reference_inst_per_s"], 2)
                      if v.get("full_reference_inst_per_s") else None)} for k, v in rk["mul_u64"].items()}
+    if "mul_u64_small" in rk:
+        sm["x_vs_ref_convMul5_small"] = {k.split("_")[0]: {
+            "truncated": round(v["truncated_ours_inst_per_s"] / v["truncated_reference_inst_per_s"], 2),
+            "full": round(v["full_ours_inst_per_s"] / v["full_reference_inst_per_s"], 2)}
+            for k, v in rk["mul_u64_small"].items()}
     if rk.get("mul2048_u32_full_reference_inst_per_s") and "mul2048_u32" in extra:
         sm["x_vs_ref_convMul5_c1"] = round(extra["mul2048_u32"]["instances_per_s"]
                                            / rk["mul2048_u32_full_reference_inst_per_s"], 2)

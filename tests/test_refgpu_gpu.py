@@ -50,7 +50,7 @@ def test_add_matches_reference_kernel(bigint, ref, m):
     assert bool((ours == rr).all())
 
 
-@pytest.mark.parametrize("m", [64, 256, 1024])
+@pytest.mark.parametrize("m", [16, 32, 64, 256, 1024])
 def test_mul_matches_reference_kernel(bigint, ref, m):
     import torch
 
@@ -70,6 +70,32 @@ def test_mul_matches_reference_kernel(bigint, ref, m):
     pb[:, :m] = db
     rf = torch.empty_like(pa)
     assert ref.lib().ref_mul_u64(pa.data_ptr(), pb.data_ptr(), rf.data_ptr(), 2 * m, n, _sp()) == 0
+    assert bool((B.mulfull(da, db) == rf).all())
+
+
+@pytest.mark.parametrize("m", [16, 32])
+def test_small_u32_mul_matches_reference_kernel(bigint, ref, m):
+    """u32 words at the small end of the reference's own multiply sweep: the
+    truncated product against convMul5 at m, the full one against convMul5 at
+    2m on zero-padded inputs (the thread and warp kernels here)."""
+    import torch
+
+    B = bigint
+    n = 512
+    a = uniform_limbs(930 + m, n, m, np.uint32)
+    b = uniform_limbs(931 + m, n, m, np.uint32)
+    a[0] = np.iinfo(np.uint32).max
+    b[0] = np.iinfo(np.uint32).max
+    da, db = B.to_device(a), B.to_device(b)
+    rr = torch.empty_like(da)
+    assert ref.lib().ref_mul_u32(da.data_ptr(), db.data_ptr(), rr.data_ptr(), m, n, _sp()) == 0
+    assert bool((B.mul(da, db) == rr).all())
+    pa = torch.zeros((n, 2 * m), dtype=torch.int32, device="cuda")
+    pb = torch.zeros_like(pa)
+    pa[:, :m] = da
+    pb[:, :m] = db
+    rf = torch.empty_like(pa)
+    assert ref.lib().ref_mul_u32(pa.data_ptr(), pb.data_ptr(), rf.data_ptr(), 2 * m, n, _sp()) == 0
     assert bool((B.mulfull(da, db) == rf).all())
 
 
