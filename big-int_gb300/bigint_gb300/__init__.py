@@ -290,7 +290,8 @@ def div(u, v, q=None, r=None, status=None, stream=None, method="auto"):
 def mul_autotune(a, b, r=None, full: bool = True, reps: int = 3, stream=None):
     """Time the CTA multiply's tilings on (a, b) -- and the 32-bit-word warp
     kernel for full products of at most 32 64-bit limbs, the one-thread-an-
-    instance kernel for products of at most 24 -- and keep the fastest for this (limb
+    instance kernel for full products of at most 24 and truncated ones of at
+    most 32 -- and keep the fastest for this (limb
     width, full, m); returns (instances per CTA, slices), (0, 0) when the warp
     kernel was fastest, (0, 1) for the thread kernel.  r receives the product
     as mulfull/mul write it."""

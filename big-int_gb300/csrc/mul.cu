@@ -309,16 +309,18 @@ static bi_status mul_thread_launch(const T* a, const T* b, T* r, uint32_t m, uin
     return check_launch(FULL ? "mulfull thread kernel" : "mul thread kernel");
 }
 
-// Products of at most MUL_THREAD_MAX_L 64-bit limbs, one thread each.
+// Products of at most MUL_THREAD_MAX_L (full) or MUL_THREAD_TRUNC_MAX_L
+// (truncated) 64-bit limbs, one thread each.
 template <typename T, bool FULL>
 static bi_status mul_thread(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     if constexpr (sizeof(T) == 4) {
         // an even word count on 8-byte-aligned buffers: the same bytes as m/2 64-bit limbs
         if (m % 2 == 0 && ((uintptr_t)a | (uintptr_t)b | (uintptr_t)r) % 8 == 0)
             return mul_thread<uint64_t, FULL>(reinterpret_cast<const uint64_t*>(a), reinterpret_cast<const uint64_t*>(b),
-                                        reinterpret_cast<uint64_t*>(r), m / 2, n, st);
+                                              reinterpret_cast<uint64_t*>(r), m / 2, n, st);
     }
-    switch (sizeof(T) == 8 ? m : (m + 1) / 2) {
+    const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
+    switch (L) {
         case 1: return mul_thread_launch<T, 1, FULL>(a, b, r, m, n, st);
         case 2: return mul_thread_launch<T, 2, FULL>(a, b, r, m, n, st);
         case 3: return mul_thread_launch<T, 3, FULL>(a, b, r, m, n, st);
@@ -343,8 +345,22 @@ static bi_status mul_thread(const T* a, const T* b, T* r, uint32_t m, uint64_t n
         case 22: return mul_thread_launch<T, 22, FULL>(a, b, r, m, n, st);
         case 23: return mul_thread_launch<T, 23, FULL>(a, b, r, m, n, st);
         case 24: return mul_thread_launch<T, 24, FULL>(a, b, r, m, n, st);
-        default: return set_error(BI_EUNSUPPORTED, "mul thread kernel: m=%u above its size", m);
+        default: break;
     }
+    if constexpr (!FULL) {
+        switch (L) {
+            case 25: return mul_thread_launch<T, 25, false>(a, b, r, m, n, st);
+            case 26: return mul_thread_launch<T, 26, false>(a, b, r, m, n, st);
+            case 27: return mul_thread_launch<T, 27, false>(a, b, r, m, n, st);
+            case 28: return mul_thread_launch<T, 28, false>(a, b, r, m, n, st);
+            case 29: return mul_thread_launch<T, 29, false>(a, b, r, m, n, st);
+            case 30: return mul_thread_launch<T, 30, false>(a, b, r, m, n, st);
+            case 31: return mul_thread_launch<T, 31, false>(a, b, r, m, n, st);
+            case 32: return mul_thread_launch<T, 32, false>(a, b, r, m, n, st);
+            default: break;
+        }
+    }
+    return set_error(BI_EUNSUPPORTED, "mul thread kernel: m=%u above its size", m);
 }
 
 // ---------------------------------------------------------------------------
@@ -431,14 +447,15 @@ template <typename T, bool FULL>
 static bi_status mul_launch(const T* a, const T* b, T* r, uint32_t m, uint64_t n, cudaStream_t st) {
     const uint32_t L = sizeof(T) == 8 ? m : (m + 1) / 2;
     if (L > MUL_MAX_L) return set_error(BI_EUNSUPPORTED, "mul: m=%u above the supported size", m);
-    if (L <= MUL_THREAD_MAX_L || (FULL && L <= MUL_WARP_MAX_L)) {
+    constexpr uint32_t THREAD_MAX = FULL ? MUL_THREAD_MAX_L : MUL_THREAD_TRUNC_MAX_L;
+    if (L <= THREAD_MAX || (FULL && L <= MUL_WARP_MAX_L)) {
         // the thread kernel (L <= MUL_THREAD_MAX_L) or, for full products, the
         // warp kernel, unless a tuning picked one of them ({0, 1}, {0, 0}) or
         // a CTA tiling
         MulTune t;
         const bool tuned = mul_tuning_lookup((int)sizeof(T), FULL, L, &t);
         if (!tuned || t.ipc == 0) {
-            const bool thread = tuned ? t.S == 1 : L <= MUL_THREAD_MAX_L;
+            const bool thread = tuned ? t.S == 1 : L <= THREAD_MAX;
             if (thread) return mul_thread<T, FULL>(a, b, r, m, n, st);
             if constexpr (FULL) return mul_warp<T>(a, b, r, m, n, st);
         }
@@ -500,7 +517,7 @@ static bi_status mul_autotune(const T* a, const T* b, T* r, uint32_t m, uint64_t
     const bool warp_ok = FULL && L <= MUL_WARP_MAX_L;
     std::vector<std::pair<uint32_t, uint32_t>> cands;
     if (warp_ok) cands.push_back({0, 0});
-    if (L <= MUL_THREAD_MAX_L) cands.push_back({0, 1});
+    if (L <= (FULL ? MUL_THREAD_MAX_L : MUL_THREAD_TRUNC_MAX_L)) cands.push_back({0, 1});
     for (uint32_t ipc = 1; ipc <= 64; ipc *= 2)
         for (uint32_t S = 1; S <= 4; S *= 2) {
             MulGeom g;
@@ -590,7 +607,8 @@ static bi_status mul_set_tuning(int limb_bytes, uint32_t m, int full, int ipc, i
         return BI_OK;
     }
     if (ipc == -1) {                                  // a per-instance kernel: slices 0 warp, 1 thread
-        const bool ok = (slices == 0 && full && L <= MUL_WARP_MAX_L) || (slices == 1 && L <= MUL_THREAD_MAX_L);
+        const bool ok = (slices == 0 && full && L <= MUL_WARP_MAX_L) ||
+                        (slices == 1 && L <= (full ? MUL_THREAD_MAX_L : MUL_THREAD_TRUNC_MAX_L));
         if (!ok) return set_error(BI_EINVAL, "mul tuning: no per-instance kernel %d for m=%u (full=%d)", slices, m, full);
         std::lock_guard<std::mutex> lk(g_tune_mu);
         g_tune[key] = {0u, (uint32_t)slices};

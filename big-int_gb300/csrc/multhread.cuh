@@ -15,7 +15,8 @@
 
 namespace bi {
 
-constexpr uint32_t MUL_THREAD_MAX_L = 24;    // largest operand, in 64-bit limbs
+constexpr uint32_t MUL_THREAD_MAX_L = 24;        // largest operand of a full product, in 64-bit limbs
+constexpr uint32_t MUL_THREAD_TRUNC_MAX_L = 32;  // of a truncated one (about half the terms)
 
 // Instances (threads) per CTA: 128, or 64 above 16 limbs, where 128 rows of
 // staged operands would pass the 48 KB of static shared memory.

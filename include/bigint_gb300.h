@@ -106,22 +106,23 @@ bi_status bi_mulfull_u32(const uint32_t* a, const uint32_t* b, uint32_t* r,
                          uint32_t m, uint64_t n, bi_stream stream);
 
 /* Tiling of the CTA multiply (64-bit limb arithmetic): instances per CTA */
-/* and row slices per window pair.  Products (full or truncated) of at    */
-/* most 24 64-bit limbs run by default on the thread kernel (one thread   */
-/* an instance, 64-bit limbs), full products of 25 to 32 limbs on the     */
-/* warp kernel (32-bit words).  bi_mul_autotune_* times every tiling that */
-/* fits on the caller's a, b -- and the warp kernel for full products of  */
-/* at most 32 64-bit limbs, the thread kernel for products of at most 24  */
-/* -- (median of `reps` runs each), records the fastest for this device,  */
-/* limb width, product kind (full != 0: bi_mulfull_*) and m, which later  */
-/* calls then use, and leaves r as that call writes it; synchronous on    */
-/* `stream`.  chosen (may be NULL) gets {instances per CTA, slices}, or   */
-/* {0, 0} when the warp kernel was fastest, {0, 1} for the thread kernel. */
-/* The reference fixes its tiling per size at compile time (ipb and the Q */
-/* limbs per thread, cuda/main.cu:15-28).  bi_mul_set_tuning_* sets a     */
-/* tiling by hand (BI_EINVAL if it does not fit a CTA); ipc = -1 picks a  */
-/* per-instance kernel (slices = 0: the warp kernel, full products of at  */
-/* most 32 limbs; 1: the thread kernel, products of at most 24); ipc = 0  */
+/* and row slices per window pair. Full products of at most 24 64-bit     */
+/* limbs and truncated ones of at most 32 run by default on the thread    */
+/* kernel (one thread an instance, 64-bit limbs), full products of 25 to  */
+/* 32 limbs on the warp kernel (32-bit words). bi_mul_autotune_* times    */
+/* every tiling that fits on the caller's a, b -- and the warp kernel for */
+/* full products of at most 32 64-bit limbs, the thread kernel where it   */
+/* takes the size -- (median of `reps` runs each), records the fastest    */
+/* for this device, limb width, product kind (full != 0: bi_mulfull_*)    */
+/* and m, which later calls then use, and leaves r as that call writes    */
+/* it; synchronous on `stream`.  chosen (may be NULL) gets {instances per */
+/* CTA, slices}, or {0, 0} when the warp kernel was fastest, {0, 1} for   */
+/* the thread kernel.  The reference fixes its tiling per size at compile */
+/* time (ipb and the Q limbs per thread, cuda/main.cu:15-28).             */
+/* bi_mul_set_tuning_* sets a tiling by hand (BI_EINVAL if it does not    */
+/* fit a CTA); ipc = -1 picks a per-instance kernel (slices = 0: the warp */
+/* kernel, full products of at most 32 limbs; 1: the thread kernel, full  */
+/* products of at most 24 limbs, truncated ones of at most 32); ipc = 0   */
 /* returns (m, full) to the library's own choice.                         */
 bi_status bi_mul_autotune_u64(const uint64_t* a, const uint64_t* b, uint64_t* r,
                               uint32_t m, uint64_t n, int full, int reps, int* chosen,

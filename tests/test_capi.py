@@ -75,7 +75,8 @@ def test_mul_tuning_arguments_checked_on_host(L):
     assert L.bi_mul_set_tuning_u64(64, 1, 4, 3) == 1                 # slices not a power of two
     assert L.bi_mul_set_tuning_u64(64, 1, 4096, 1) == 1              # more instances than a CTA holds
     assert L.bi_mul_set_tuning_u64(64, 1, -1, 1) == 1                # no per-instance kernel at 64 limbs
-    assert L.bi_mul_set_tuning_u64(25, 1, -1, 1) == 1                # thread kernel: at most 24 limbs
+    assert L.bi_mul_set_tuning_u64(25, 1, -1, 1) == 1                # thread kernel: full products up to 24 limbs
+    assert L.bi_mul_set_tuning_u64(33, 0, -1, 1) == 1                # and truncated ones up to 32
     assert L.bi_mul_set_tuning_u64(8, 1, -1, 2) == 1                 # no such per-instance kernel
     assert L.bi_mul_set_tuning_u64(8, 0, -1, 0) == 1                 # truncated products: no warp kernel
     assert L.bi_mul_set_tuning_u64(8, 1, -2, 1) == 1

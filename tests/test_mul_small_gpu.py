@@ -1,6 +1,6 @@
 """Products of at most 32 64-bit limbs on the per-instance kernels: the
 thread kernel (one thread an instance, 64-bit limbs; the default for full
-and truncated products up to 24 limbs) and the warp kernel (32-bit words;
+products up to 24 limbs and truncated ones up to 32) and the warp kernel (32-bit words;
 full products only, the default from 25 to 32 limbs), each pinned by hand at
 every size it takes, both limb widths, against the oracle: saturated
 columns, zeros, single bits, ragged last tiles, and a batch larger than one
@@ -13,6 +13,7 @@ from bigint_gb300.workloads import uniform_limbs
 pytestmark = pytest.mark.gpu
 
 THREAD_MAX_L = 24
+THREAD_TRUNC_MAX_L = 32
 WARP_MAX_L = 32
 
 
@@ -52,7 +53,7 @@ def _reset(bigint):
                                          ("default", False), ("thread", False)])
 def test_every_small_size(bigint, oracle, dtype, kernel, full):
     B = bigint
-    top_m = THREAD_MAX_L if kernel == "thread" or not full else WARP_MAX_L
+    top_m = (THREAD_MAX_L if kernel == "thread" else WARP_MAX_L) if full else THREAD_TRUNC_MAX_L
     sizes = range(1, (top_m if dtype == np.uint64 else 2 * top_m) + 1)
     for m in sizes:
         if kernel != "default":
@@ -70,7 +71,7 @@ def test_every_small_size(bigint, oracle, dtype, kernel, full):
 
 @pytest.mark.parametrize("full", [True, False])
 @pytest.mark.parametrize("m,dtype", [(1, np.uint64), (3, np.uint32), (16, np.uint64), (31, np.uint32), (24, np.uint64),
-                                     (47, np.uint32)])
+                                     (47, np.uint32), (32, np.uint64), (63, np.uint32)])
 def test_batch_larger_than_the_grid(bigint, m, dtype, full):
     """More instances than the capped grid holds at once (152 SMs x CTAs an SM
     x 128 or 64 instances): rows in every wave, checked as Python integers."""
@@ -137,7 +138,7 @@ def test_pinning_checked(bigint):
     with pytest.raises(B.BigIntError):
         B.mul_set_tuning(8, np.uint64, False, -1, 0)        # truncated products: no warp kernel
     with pytest.raises(B.BigIntError):
-        B.mul_set_tuning(25, np.uint64, False, -1, 1)       # thread kernel above 24 limbs
+        B.mul_set_tuning(33, np.uint64, False, -1, 1)       # truncated: thread kernel above 32 limbs
     B.mul_set_tuning(33, np.uint32, True, -1, 0)            # 17 64-bit limbs on the warp kernel: fine
     B.mul_set_tuning(48, np.uint32, True, -1, 1)            # 24 64-bit limbs on the thread kernel: fine
-    B.mul_set_tuning(24, np.uint64, False, -1, 1)           # truncated, on the thread kernel: fine
+    B.mul_set_tuning(32, np.uint64, False, -1, 1)           # truncated, on the thread kernel: fine
