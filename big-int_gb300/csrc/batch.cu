@@ -196,11 +196,16 @@ batch_mulwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restri
 }
 
 // division classes by divisor limbs: long division on threads (divisors up
-// to 4, 8, 16 limbs), on warps (up to 32, 64, ..., 1024 limbs), block long
-// division on two warps (up to 2048 limbs) and four warps (up to 4096); the
-// shifted inverse on 512-thread CTAs is the class that a size class above
-// 128 limbs with few divisions runs as
-constexpr int DIV_THREAD_CLASSES = 3, DIV_WARP_CLASSES = 6;
+// to 4, 8, 16 limbs), on warps or lane groups (up to 32, 64, 128, 256, 384,
+// 512, 768, 1024 limbs: a divisor is right-aligned in its lanes' blocks,
+// whose rows below it are zeros, so 384 takes 16-lane groups of 24 limbs
+// and 768 a warp of 24 limbs a lane where 512 and 1024 take warps of 16 and
+// 32), block long division on two warps (up
+// to 2048 limbs) and four warps (up to 4096); the shifted inverse on
+// 512-thread CTAs is the class that a size class above 128 limbs with few
+// divisions runs as
+constexpr int DIV_THREAD_CLASSES = 3, DIV_WARP_CLASSES = 8;
+constexpr uint32_t DIV_WARP_CLASS_MAX_MV[DIV_WARP_CLASSES] = {32, 64, 128, 256, 384, 512, 768, 1024};
 constexpr int DIV_CTA_CLASS = DIV_THREAD_CLASSES + DIV_WARP_CLASSES;
 constexpr int DIV_BLK2_CLASS = DIV_CTA_CLASS + 1, DIV_BLK4_CLASS = DIV_CTA_CLASS + 2;
 constexpr int DIV_CLASSES = DIV_CTA_CLASS + 3;
@@ -214,9 +219,9 @@ static inline int div_class(uint32_t mv) {
     if (mv <= 8) return 1;
     if (mv <= 16) return 2;
     if (mv > (uint32_t)DIV_WARP_MAX_MV) return mv <= 2048 ? DIV_BLK2_CLASS : DIV_BLK4_CLASS;
-    int c = DIV_THREAD_CLASSES;
-    for (uint32_t cap = 32; cap < mv; cap *= 2) c++;
-    return c;
+    int c = 0;
+    while (DIV_WARP_CLASS_MAX_MV[c] < mv) c++;
+    return DIV_THREAD_CLASSES + c;
 }
 
 template <int MX>
@@ -431,7 +436,7 @@ static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n,
     for (int c = 0; c < DIV_CLASSES; c++) {
         map[c] = c;
         if (c >= DIV_THREAD_CLASSES && c < DIV_CTA_CLASS && max_m[c] <= BATCH_SHINV_MAX_M) {
-            const uint32_t max_mv = 32u << (c - DIV_THREAD_CLASSES);   // the class's largest divisor
+            const uint32_t max_mv = DIV_WARP_CLASS_MAX_MV[c - DIV_THREAD_CLASSES];   // the class's largest divisor
             if (max_mv > 128) {
                 const uint64_t per_sm = max_mv <= 256 ? 2 : max_mv <= 512 ? 3 : 6;
                 if (cnt[c] <= per_sm * (uint64_t)sms) map[c] = DIV_CTA_CLASS;
@@ -494,8 +499,10 @@ static const void* div_class_kernel(int c, int* threads) {
     case 4: return (const void*)batch_divgroup_kernel<8, 8>;
     case 5: return (const void*)batch_divgroup_kernel<8, 16>;
     case 6: return (const void*)batch_divwarp_kernel<8>;
-    case 7: return (const void*)batch_divwarp_kernel<16>;
-    case 8: return (const void*)batch_divwarp_kernel<32>;
+    case 7: return (const void*)batch_divgroup_kernel<24, 16>;
+    case 8: return (const void*)batch_divwarp_kernel<16>;
+    case 9: return (const void*)batch_divwarp_kernel<24>;
+    case 10: return (const void*)batch_divwarp_kernel<32>;
     default: return (const void*)batch_div_kernel<DIV_CTA_THREADS>;
     }
 }
@@ -556,7 +563,7 @@ static bi_status prepare_launch(bi_plan* p, const BatchTune& t, Launch3* L) {
         int threads = 0;
         const void* k = div_class_kernel(c, &threads);
         // instances per CTA: one a thread, one a lane group (8, 16 or 32 lanes), one a CTA
-        static constexpr uint32_t group_ipw[DIV_WARP_CLASSES] = {4, 4, 2, 1, 1, 1};
+        static constexpr uint32_t group_ipw[DIV_WARP_CLASSES] = {4, 4, 2, 1, 2, 1, 1, 1};
         const uint64_t per = c < DIV_THREAD_CLASSES ? (uint64_t)threads
                              : c < DIV_CTA_CLASS    ? (uint64_t)threads / 32 * group_ipw[c - DIV_THREAD_CLASSES]
                                                     : 1;
@@ -626,8 +633,10 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
             case 4: batch_divgroup_kernel<8, 8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 5: batch_divgroup_kernel<8, 16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 6: batch_divwarp_kernel<8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
-            case 7: batch_divwarp_kernel<16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
-            case 8: batch_divwarp_kernel<32><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 7: batch_divgroup_kernel<24, 16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 8: batch_divwarp_kernel<16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 9: batch_divwarp_kernel<24><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 10: batch_divwarp_kernel<32><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case DIV_BLK2_CLASS: batch_divblk_kernel<2><<<grid, 64, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case DIV_BLK4_CLASS: batch_divblk_kernel<4><<<grid, 128, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             default:

@@ -340,6 +340,45 @@ def test_large_divisions_in_a_batch(bigint, oracle):
     plan.close()
 
 
+def test_division_lane_classes_in_a_batch(bigint):
+    """Divisions of 2m by m limbs for divisors on either side of the batch's
+    lane-width classes (16-lane groups of 24 limbs up to 384, warps of 16
+    limbs up to 512, of 24 up to 768 and of 32 up to 1024), enough of each
+    class that none runs as the shifted inverse; checked as Python
+    integers (u = q v + r, r < v)."""
+    B = bigint
+    rng = np.random.default_rng(91)
+    shapes = [(mv, 160) for mv in (257, 300, 384, 385, 450, 512)] + [(mv, 310) for mv in (513, 600, 768, 769, 900, 1024)]
+    ops = [mv for mv, k in shapes for _ in range(k)]
+    d = np.zeros(len(ops), dtype=B.DESC_DTYPE)
+    pos = out = 0
+    for i, mv in enumerate(ops):
+        m = 2 * mv
+        d[i]["op"], d[i]["m"], d[i]["mb"] = B.OP_DIV, m, mv
+        d[i]["a"], d[i]["b"] = pos, pos + m
+        pos += m + mv
+        d[i]["r"], d[i]["r2"] = out, out + m
+        out += m + mv
+        d[i]["flag"] = i
+    arena = rng.integers(0, 2**64, size=pos, dtype=np.uint64)
+    for i, mv in enumerate(ops):
+        b = int(d[i]["b"])
+        arena[b + mv - 1] |= np.uint64(1)
+        if i % 97 == 0:                                   # all-ones operands
+            arena[int(d[i]["a"]): b + mv] = np.uint64(0xFFFFFFFFFFFFFFFF)
+    plan, din, dout, dfl = _run(B, d, arena, out, len(ops))
+    res = B.to_host(dout, np.uint64)
+    assert (dfl.cpu().numpy()[: len(ops)] == 0).all()
+    for i, mv in enumerate(ops):
+        a, b, r, r2 = int(d[i]["a"]), int(d[i]["b"]), int(d[i]["r"]), int(d[i]["r2"])
+        U = int.from_bytes(arena[a: a + 2 * mv].tobytes(), "little")
+        V = int.from_bytes(arena[b: b + mv].tobytes(), "little")
+        Q = int.from_bytes(res[r: r + 2 * mv].tobytes(), "little")
+        R = int.from_bytes(res[r2: r2 + mv].tobytes(), "little")
+        assert Q * V + R == U and R < V, (mv, i)
+    plan.close()
+
+
 def test_batch_size_limits_rejected(bigint):
     """Sizes past the batch's limits are refused when the plan is built."""
     B = bigint

@@ -128,6 +128,37 @@ def test_method_boundaries(bigint, oracle, mu, mv):
         _run(bigint, oracle, u, v, method)
 
 
+@pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
+@pytest.mark.parametrize("method,n", [("long", 37), ("auto", 1000)])
+def test_lane_width_boundaries(bigint, dtype, method, n):
+    """Divisors on either side of each lane width of long division -- 16-lane
+    groups of 24 and 32 limbs (up to 384 and 512 limbs), warps of 24 and 32
+    limbs a lane (up to 768 and 1024) -- with 2m-limb dividends, shorter
+    divisors in a wider row, all-ones operands and dividends below the
+    divisor; checked as Python integers (u = q v + r, r < v)."""
+    B = bigint
+    w = 2 if dtype == np.uint32 else 1
+    bits = 8 * np.dtype(dtype).itemsize
+    for mv in (256, 257, 384, 385, 512, 513, 768, 769, 1024):
+        u = uniform_limbs(700 + mv, n, 2 * mv * w, dtype)
+        v = uniform_limbs(701 + mv, n, mv * w, dtype)
+        v[:, -1] |= 1
+        v[1, (mv * w) // 2:] = 0
+        v[1, (mv * w) // 2 - 1] |= 1
+        u[2] = np.iinfo(dtype).max
+        v[2] = np.iinfo(dtype).max
+        u[3, mv * w:] = 0                          # u < v
+        q, r, st = B.div(B.to_device(u), B.to_device(v), method=method)
+        q, r = B.to_host(q, dtype), B.to_host(r, dtype)
+        assert (st.cpu().numpy() == 0).all()
+        for i in range(n):
+            U = int.from_bytes(u[i].tobytes(), "little")
+            V = int.from_bytes(v[i].tobytes(), "little")
+            Q = int.from_bytes(q[i].tobytes(), "little")
+            R = int.from_bytes(r[i].tobytes(), "little")
+            assert Q * V + R == U and R < V, (mv, i, bits)
+
+
 def test_size_limits_rejected(bigint):
     """Dividends above 8192 64-bit limbs, shifted-inverse dividends above 2048
     and long-division divisors above 4096 are refused before any launch."""
