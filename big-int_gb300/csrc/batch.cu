@@ -200,7 +200,9 @@ batch_mulwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restri
 // 512, 768, 1024 limbs: a divisor is right-aligned in its lanes' blocks,
 // whose rows below it are zeros, so 384 takes 16-lane groups of 24 limbs
 // and 768 a warp of 24 limbs a lane where 512 and 1024 take warps of 16 and
-// 32), block long division on two warps (up
+// 32; finer classes, of 20 and 28 limbs a lane, were 2 % slower on the
+// 100000-instance batch: two more persistent kernels sharing the SMs),
+// block long division on two warps (up
 // to 2048 limbs) and four warps (up to 4096); the shifted inverse on
 // 512-thread CTAs is the class that a size class above 128 limbs with few
 // divisions runs as
@@ -418,13 +420,19 @@ static size_t mul_smem_for(const bi_plan* p, int ipc_div) {
 }
 
 // The class of each division: by divisor size (div_class), except that a
-// class above 128 limbs with too few divisions for long division's
-// throughput to win goes to the shifted inverse on CTAs: at most 2, 3 and 6
-// per SM for divisors up to 256, 512 and 1024 limbs.  (Up to 128 limbs long
-// division stays: beside the batch's other kernels its small lane groups
-// pack where a CTA per division does not -- a 20000-instance batch ran
-// 1.74 ms so and 1.94 ms with the uniform entry's crossover.)  map[c] is the
-// class that size class c runs as.
+// band of divisor sizes above 128 limbs (129-256, 257-512, 513-1024) with too
+// few divisions for long division's throughput to win goes to the shifted
+// inverse on CTAs: at most 2, 3 and 6 per SM in the band.  The band, not the
+// class, is counted: the classes that split a band (384 and 512; 768 and
+// 1024) each hold a share of its divisions, and counting them one by one
+// sent classes of a 100000-instance batch that split the 513-1024 band more
+// finely to the shifted inverse (15.9M -> 13.5M instances/s).  (Up to 128 limbs long division
+// stays: beside the batch's other kernels its small lane groups pack where
+// a CTA per division does not -- a 20000-instance batch ran 1.74 ms so and
+// 1.94 ms with the uniform entry's crossover.)  map[c] is the class that
+// size class c runs as.
+static uint32_t div_band(uint32_t max_mv) { return max_mv <= 256 ? 256 : max_mv <= 512 ? 512 : 1024; }
+
 static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n, int sms, int* map) {
     uint64_t cnt[DIV_CLASSES] = {};
     uint32_t max_m[DIV_CLASSES] = {};
@@ -438,8 +446,14 @@ static void div_class_map(const bi_desc* descs, const uint32_t* div, uint32_t n,
         if (c >= DIV_THREAD_CLASSES && c < DIV_CTA_CLASS && max_m[c] <= BATCH_SHINV_MAX_M) {
             const uint32_t max_mv = DIV_WARP_CLASS_MAX_MV[c - DIV_THREAD_CLASSES];   // the class's largest divisor
             if (max_mv > 128) {
-                const uint64_t per_sm = max_mv <= 256 ? 2 : max_mv <= 512 ? 3 : 6;
-                if (cnt[c] <= per_sm * (uint64_t)sms) map[c] = DIV_CTA_CLASS;
+                const uint32_t band = div_band(max_mv);
+                uint64_t band_cnt = 0;
+                for (int b = DIV_THREAD_CLASSES; b < DIV_CTA_CLASS; b++) {
+                    const uint32_t bmv = DIV_WARP_CLASS_MAX_MV[b - DIV_THREAD_CLASSES];
+                    if (bmv > 128 && div_band(bmv) == band) band_cnt += cnt[b];
+                }
+                const uint64_t per_sm = band == 256 ? 2 : band == 512 ? 3 : 6;
+                if (band_cnt <= per_sm * (uint64_t)sms) map[c] = DIV_CTA_CLASS;
             }
         }
     }

@@ -160,19 +160,23 @@ __device__ __forceinline__ uint32_t chain_add_gen(uint64_t* x, Gen gen, uint32_t
 
 // x = x - (gen(0), gen(1), ...) - c over N limbs, the subtrahend produced
 // eight limbs at a time just before its chain block, so that no more than
-// eight of its limbs are live at once.
+// eight of its limbs are live at once (any N: a length that is not 1, 2, 4
+// or a multiple of 8 ends in blocks of 4, 2 and 1, as chain_sub_gen does).
 template <int N, typename Gen>
 __device__ __forceinline__ uint32_t chain_sub_from(uint64_t (&x)[N], Gen gen, uint32_t c) {
     constexpr int Bk = N < 8 ? N : 8;
-    static_assert(N % Bk == 0, "chain_sub_from: N must be 1, 2, 4 or a multiple of 8");
+    if constexpr (N % Bk != 0 || (N < 8 && N != 1 && N != 2 && N != 4)) {
+        return chain_sub_gen<N>(&x[0], gen, c);
+    } else {
 #pragma unroll
-    for (int b = 0; b < N / Bk; b++) {
-        uint64_t y[Bk];
+        for (int b = 0; b < N / Bk; b++) {
+            uint64_t y[Bk];
 #pragma unroll
-        for (int j = 0; j < Bk; j++) y[j] = gen(b * Bk + j);
-        c = chain_sub<Bk>(*reinterpret_cast<uint64_t(*)[Bk]>(&x[b * Bk]), y, c);
+            for (int j = 0; j < Bk; j++) y[j] = gen(b * Bk + j);
+            c = chain_sub<Bk>(*reinterpret_cast<uint64_t(*)[Bk]>(&x[b * Bk]), y, c);
+        }
+        return c;
     }
-    return c;
 }
 
 // The carry out alone (x and y unchanged): the same chain on copies.

@@ -192,11 +192,14 @@ static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status,
     else if (MV <= 64) div_group_kernel<T, 8, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 128) div_group_kernel<T, 8, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 256) div_warp_kernel<T, 8><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
-    // 24 limbs a lane below 3/4 of the power of two: a divisor is right-aligned
-    // in the lanes' 32 VPL (or G VPL) limbs, whose rows below it are zeros
+    // 20, 24 and 28 limbs a lane between the powers of two: a divisor is
+    // right-aligned in the lanes' 32 VPL (or G VPL) limbs, whose rows below it
+    // are zeros
     else if (MV <= 384) div_group_kernel<T, 24, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 512) div_group_kernel<T, 32, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 640) div_warp_kernel<T, 20><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 768) div_warp_kernel<T, 24><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 896) div_warp_kernel<T, 28><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else div_warp_kernel<T, 32><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
 }
 

@@ -132,14 +132,14 @@ def test_method_boundaries(bigint, oracle, mu, mv):
 @pytest.mark.parametrize("method,n", [("long", 37), ("auto", 1000)])
 def test_lane_width_boundaries(bigint, dtype, method, n):
     """Divisors on either side of each lane width of long division -- 16-lane
-    groups of 24 and 32 limbs (up to 384 and 512 limbs), warps of 24 and 32
-    limbs a lane (up to 768 and 1024) -- with 2m-limb dividends, shorter
+    groups of 24 and 32 limbs (up to 384 and 512 limbs), warps of 20, 24, 28
+    and 32 limbs a lane (up to 640, 768, 896 and 1024) -- with 2m-limb dividends, shorter
     divisors in a wider row, all-ones operands and dividends below the
     divisor; checked as Python integers (u = q v + r, r < v)."""
     B = bigint
     w = 2 if dtype == np.uint32 else 1
     bits = 8 * np.dtype(dtype).itemsize
-    for mv in (256, 257, 384, 385, 512, 513, 768, 769, 1024):
+    for mv in (256, 257, 384, 385, 512, 513, 640, 641, 768, 769, 896, 897, 1024):
         u = uniform_limbs(700 + mv, n, 2 * mv * w, dtype)
         v = uniform_limbs(701 + mv, n, mv * w, dtype)
         v[:, -1] |= 1
