@@ -251,9 +251,9 @@ batch_divthread_kernel(const bi_desc* __restrict__ descs, const uint32_t* __rest
 }
 
 template <int VPL>
-__global__ void __launch_bounds__(DIV_WARP_CTA)
-batch_divwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
-                     uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+__device__ __forceinline__ void batch_divwarp_items(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list,
+                                                    uint32_t count, uint32_t* counter, const uint64_t* in, uint64_t* out,
+                                                    uint8_t* flags) {
     const uint32_t lane = threadIdx.x & 31;
     for (;;) {
         uint32_t idx = 0;
@@ -270,6 +270,22 @@ batch_divwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restri
             m64(d), mb64(d), lu, lv, sq, sr);
         if (flags && lane == 0) flags[d.flag] = st;
     }
+}
+
+template <int VPL>
+__global__ void __launch_bounds__(DIV_WARP_CTA)
+batch_divwarp_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                     uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    batch_divwarp_items<VPL>(descs, list, count, counter, in, out, flags);
+}
+
+// Held to three CTAs (12 warps) an SM, for 24 limbs a lane (as the uniform
+// entry's div_warp3_kernel): 168 registers instead of 194.
+template <int VPL>
+__global__ void __launch_bounds__(DIV_WARP_CTA, 3)
+batch_divwarp3_kernel(const bi_desc* __restrict__ descs, const uint32_t* __restrict__ list, uint32_t count,
+                      uint32_t* counter, const uint64_t* in, uint64_t* out, uint8_t* flags) {
+    batch_divwarp_items<VPL>(descs, list, count, counter, in, out, flags);
 }
 
 // Several divisions a warp, one per G-lane group (div_group): lane 0 takes
@@ -515,7 +531,7 @@ static const void* div_class_kernel(int c, int* threads) {
     case 6: return (const void*)batch_divwarp_kernel<8>;
     case 7: return (const void*)batch_divgroup_kernel<24, 16>;
     case 8: return (const void*)batch_divwarp_kernel<16>;
-    case 9: return (const void*)batch_divwarp_kernel<24>;
+    case 9: return (const void*)batch_divwarp3_kernel<24>;
     case 10: return (const void*)batch_divwarp_kernel<32>;
     default: return (const void*)batch_div_kernel<DIV_CTA_THREADS>;
     }
@@ -649,7 +665,7 @@ static bi_status launch_plan_kernels(bi_plan* p, const uint64_t* in, uint64_t* o
             case 6: batch_divwarp_kernel<8><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 7: batch_divgroup_kernel<24, 16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 8: batch_divwarp_kernel<16><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
-            case 9: batch_divwarp_kernel<24><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
+            case 9: batch_divwarp3_kernel<24><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case 10: batch_divwarp_kernel<32><<<grid, DIV_WARP_CTA, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case DIV_BLK2_CLASS: batch_divblk_kernel<2><<<grid, 64, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;
             case DIV_BLK4_CLASS: batch_divblk_kernel<4><<<grid, 128, 0, st>>>(p->d_descs, list, n, ctr, in, out, flags); break;

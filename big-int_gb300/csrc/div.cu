@@ -125,9 +125,9 @@ static void launch_div_thread(const T* u, const T* v, T* q, T* r, uint8_t* statu
 // One warp per instance: long division for divisors of at most 32 VPL limbs
 // (divsmall.cuh).
 template <typename T, int VPL>
-__global__ void __launch_bounds__(DIV_WARP_CTA)
-div_warp_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
-                uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
+__device__ __forceinline__ void div_warp_instances(const T* __restrict__ u, const T* __restrict__ v,
+                                                   T* __restrict__ q, T* __restrict__ r,
+                                                   uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
     const uint32_t MU = sizeof(T) == 8 ? mu : (mu + 1) / 2, MV = sizeof(T) == 8 ? mv : (mv + 1) / 2;
     const uint64_t warps = (uint64_t)gridDim.x * (DIV_WARP_CTA / 32);
     for (uint64_t inst = (uint64_t)blockIdx.x * (DIV_WARP_CTA / 32) + threadIdx.x / 32; inst < n; inst += warps) {
@@ -141,6 +141,25 @@ div_warp_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict_
             [&](uint32_t i, uint64_t x) { put_limb64(ri, mv, i, x); });
         if (status && (threadIdx.x & 31) == 0) status[inst] = st;
     }
+}
+
+template <typename T, int VPL>
+__global__ void __launch_bounds__(DIV_WARP_CTA)
+div_warp_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
+                uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
+    div_warp_instances<T, VPL>(u, v, q, r, status, n, mu, mv);
+}
+
+// The same, held to three CTAs (12 warps) an SM: for 24 limbs a lane, where
+// ptxas otherwise takes 255 registers (8 warps an SM), 168 registers and a
+// few spills ran 4-10 % faster (700- and 768-limb divisors); the 20- and
+// 28-limb shapes stay on the default bound (their 3-CTA variants were slower
+// or spilled 240 bytes).
+template <typename T, int VPL>
+__global__ void __launch_bounds__(DIV_WARP_CTA, 3)
+div_warp3_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict__ q, T* __restrict__ r,
+                 uint8_t* __restrict__ status, uint64_t n, uint32_t mu, uint32_t mv) {
+    div_warp_instances<T, VPL>(u, v, q, r, status, n, mu, mv);
 }
 
 template <typename T, int VPL, int G>
@@ -198,7 +217,7 @@ static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status,
     else if (MV <= 384) div_group_kernel<T, 24, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 512) div_group_kernel<T, 32, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 640) div_warp_kernel<T, 20><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
-    else if (MV <= 768) div_warp_kernel<T, 24><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 768) div_warp3_kernel<T, 24><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 896) div_warp_kernel<T, 28><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else div_warp_kernel<T, 32><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
 }
