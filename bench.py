@@ -459,7 +459,9 @@ def measure_extra(B, L, stream, args):
     div = {}
     # 2^23 dividend limbs a size: dividends, divisors, quotients and remainders (192 MB) pass
     # the 129 MB L2, so the small sizes are timed on memory, not on one ~10 us launch
-    for mv, n in [(4, 1 << 20), (16, 1 << 18), (64, 1 << 16), (256, 1 << 14), (1024, 1 << 12)]:
+    # 384 and 768: divisors between the powers of two, on the 24-limb-a-lane shapes
+    for mv, n in [(4, 1 << 20), (16, 1 << 18), (64, 1 << 16), (256, 1 << 14), (384, (1 << 23) // 768),
+                  (768, (1 << 23) // 1536), (1024, 1 << 12)]:
         u = device_uniform_u64(11, n, 2 * mv)
         v = device_uniform_u64(12, n, mv)
         v[:, -1] |= 1

@@ -258,7 +258,8 @@ def test_exact_where_reference_prototype_is_one_short(bigint, oracle):
     assert sum(int(x) << (32 * i) for i, x in enumerate(qf[0])) == U // V - 1
 
 
-@pytest.mark.parametrize("mv,n", [(4, 1 << 20), (16, 1 << 18), (64, 1 << 16), (256, 1 << 14), (1024, 1 << 12)])
+@pytest.mark.parametrize("mv,n", [(4, 1 << 20), (16, 1 << 18), (64, 1 << 16), (256, 1 << 14), (384, (1 << 23) // 768),
+                                  (768, (1 << 23) // 1536), (1024, 1 << 12)])
 def test_full_size_division_identity(bigint, mv, n):
     """The benchmark's division workloads at full size (2m/m limbs, u64),
     checked on every row by a property the division kernels do not share:
