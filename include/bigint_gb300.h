@@ -158,10 +158,11 @@ bi_status bi_div_u32(const uint32_t* u, const uint32_t* v, uint32_t* q, uint32_t
                      bi_stream stream);
 /* The method depends on the divisor's size in 64-bit limbs and on n (the */
 /* results do not: q and r are unique): schoolbook long division on one   */
-/* thread per instance up to 16 limbs and on one warp per instance up to  */
-/* 128 limbs, and up to 1024 limbs once n exceeds a few instances per SM  */
-/* (otherwise the shifted inverse on one CTA per instance); above 1024    */
-/* limbs long division 8 quotient limbs at a time on two or four warps.   */
+/* thread per instance up to 16 limbs and on one warp or lane group (8 or */
+/* 16 lanes, 1 to 32 limbs a lane) per instance up to 128 limbs, and up   */
+/* to 1024 limbs once n exceeds a few instances per SM (otherwise the     */
+/* shifted inverse on one CTA per instance); above 1024 limbs long        */
+/* division 8 quotient limbs at a time on two or four warps.              */
 /* The _shinv entries take the shifted inverse at every size (the         */
 /* reference's algorithm; dividends up to 2048 64-bit limbs, else         */
 /* BI_EUNSUPPORTED), the _long entries long division (divisors up to 4096 */
