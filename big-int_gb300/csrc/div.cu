@@ -189,8 +189,9 @@ div_group_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict
 // divisor size that ran fastest on GB300 (2m/m divisions, thousands of
 // instances): 8-lane groups of 4 and 8 limbs a lane up to 32 and 64 limbs,
 // 16-lane groups of 8 up to 128, a whole warp of 8 up to 256, 16-lane groups
-// of 32 up to 512, a warp of 32 up to 1024; with few instances
-// (div_small_on_warps) one warp each up to 128 limbs.
+// of 24 and 32 up to 384 and 512, a warp of 20, 24, 28 and 32 up to 640,
+// 768, 896 and 1024; with few instances (div_small_on_warps) one warp each
+// up to 128 limbs.
 template <typename T>
 static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
                             uint64_t n, cudaStream_t s) {
