@@ -187,11 +187,13 @@ div_group_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict
 
 // Long division for divisors of 17..1024 64-bit limbs: the group shape per
 // divisor size that ran fastest on GB300 (2m/m divisions, thousands of
-// instances): 8-lane groups of 4 and 8 limbs a lane up to 32 and 64 limbs,
-// 16-lane groups of 8 up to 128, a whole warp of 8 up to 256, 16-lane groups
-// of 24 and 32 up to 384 and 512, a warp of 20, 24, 28 and 32 up to 640,
-// 768, 896 and 1024; with few instances (div_small_on_warps) one warp each
-// up to 128 limbs.
+// instances): 8-lane groups of 4, 6 and 8 limbs a lane up to 32, 48 and 64
+// limbs, 16-lane groups of 6 and 8 up to 96 and 128, a whole warp of 6 and 8
+// up to 192 and 256, 16-lane groups of 24 and 32 up to 384 and 512, a warp
+// of 20, 24, 28 and 32 up to 640, 768, 896 and 1024 (the shapes between the
+// powers of two run 1.1-1.4x faster there: fewer rows of zeros below the
+// right-aligned divisor, fewer registers); with few instances
+// (div_small_on_warps) one warp each up to 128 limbs.
 template <typename T>
 static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
                             uint64_t n, cudaStream_t s) {
@@ -209,8 +211,11 @@ static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status,
         return;
     }
     if (MV <= 32) div_group_kernel<T, 4, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 48) div_group_kernel<T, 6, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 64) div_group_kernel<T, 8, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 96) div_group_kernel<T, 6, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 128) div_group_kernel<T, 8, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 192) div_warp_kernel<T, 6><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 256) div_warp_kernel<T, 8><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     // 20, 24 and 28 limbs a lane between the powers of two: a divisor is
     // right-aligned in the lanes' 32 VPL (or G VPL) limbs, whose rows below it

@@ -159,6 +159,34 @@ def test_lane_width_boundaries(bigint, dtype, method, n):
             assert Q * V + R == U and R < V, (mv, i, bits)
 
 
+@pytest.mark.parametrize("dtype", [np.uint64, np.uint32])
+def test_small_lane_shape_boundaries(bigint, dtype):
+    """Divisors on either side of the lane-group shapes below 256 limbs (8-lane
+    groups of 4, 6, 8 limbs up to 32, 48, 64; 16-lane groups of 6 and 8 up to
+    96 and 128; warps of 6 and 8 up to 192 and 256), with enough instances
+    (2000) that the groups run; checked as Python integers."""
+    B = bigint
+    w = 2 if dtype == np.uint32 else 1
+    n = 2000
+    for mv in (32, 33, 48, 49, 64, 65, 96, 97, 128, 129, 192, 193):
+        u = uniform_limbs(800 + mv, n, 2 * mv * w, dtype)
+        v = uniform_limbs(801 + mv, n, mv * w, dtype)
+        v[:, -1] |= 1
+        v[1::9, (mv * w) // 2:] = 0
+        v[1::9, (mv * w) // 2 - 1] |= 1
+        u[2::13] = np.iinfo(dtype).max
+        v[2::13] = np.iinfo(dtype).max
+        q, r, st = B.div(B.to_device(u), B.to_device(v), method="long")
+        q, r = B.to_host(q, dtype), B.to_host(r, dtype)
+        assert (st.cpu().numpy() == 0).all()
+        for i in range(0, n, 7):
+            U = int.from_bytes(u[i].tobytes(), "little")
+            V = int.from_bytes(v[i].tobytes(), "little")
+            Q = int.from_bytes(q[i].tobytes(), "little")
+            R = int.from_bytes(r[i].tobytes(), "little")
+            assert Q * V + R == U and R < V, (mv, i)
+
+
 def test_size_limits_rejected(bigint):
     """Dividends above 8192 64-bit limbs, shifted-inverse dividends above 2048
     and long-division divisors above 4096 are refused before any launch."""
