@@ -193,12 +193,12 @@ div_group_kernel(const T* __restrict__ u, const T* __restrict__ v, T* __restrict
 
 // Long division for divisors of 17..1024 64-bit limbs: the group shape per
 // divisor size that ran fastest on GB300 (2m/m divisions, thousands of
-// instances): 8-lane groups of 4, 6 and 8 limbs a lane up to 32, 48 and 64
-// limbs, 16-lane groups of 6 and 8 up to 96 and 128, a whole warp of 6 and 8
-// up to 192 and 256, 16-lane groups of 24 and 32 up to 384 and 512, a warp
-// of 20, 24, 28 and 32 up to 640, 768, 896 and 1024 (the shapes between the
-// powers of two run 1.1-1.4x faster there: fewer rows of zeros below the
-// right-aligned divisor, fewer registers); with few instances
+// instances): 8-lane groups of 3, 4, 6 and 8 limbs a lane up to 24, 32, 48
+// and 64 limbs, 16-lane groups of 6 and 8 up to 96 and 128, a whole warp of 6
+// and 8 up to 192 and 256, 16-lane groups of 20, 24, 28 and 32 up to 320,
+// 384, 448 and 512, a warp of 20, 24, 28 and 32 up to 640, 768, 896 and 1024
+// (the shapes between the powers of two run 1.07-1.4x faster there: fewer
+// rows of zeros below the right-aligned divisor, fewer registers); with few instances
 // (div_small_on_warps) one warp each up to 128 limbs.
 template <typename T>
 static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status, uint32_t mu, uint32_t mv,
@@ -216,7 +216,8 @@ static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status,
         else div_warp_kernel<T, 4><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
         return;
     }
-    if (MV <= 32) div_group_kernel<T, 4, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    if (MV <= 24) div_group_kernel<T, 3, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 32) div_group_kernel<T, 4, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 48) div_group_kernel<T, 6, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 64) div_group_kernel<T, 8, 8><<<grid_for(4), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 96) div_group_kernel<T, 6, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
@@ -226,7 +227,9 @@ static void launch_div_warp(const T* u, const T* v, T* q, T* r, uint8_t* status,
     // 20, 24 and 28 limbs a lane between the powers of two: a divisor is
     // right-aligned in the lanes' 32 VPL (or G VPL) limbs, whose rows below it
     // are zeros
+    else if (MV <= 320) div_group_kernel<T, 20, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 384) div_group_kernel<T, 24, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
+    else if (MV <= 448) div_group_kernel<T, 28, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 512) div_group_kernel<T, 32, 16><<<grid_for(2), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 640) div_warp_kernel<T, 20><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);
     else if (MV <= 768) div_warp3_kernel<T, 24><<<grid_for(1), DIV_WARP_CTA, 0, s>>>(u, v, q, r, status, n, mu, mv);

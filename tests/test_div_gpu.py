@@ -139,7 +139,7 @@ def test_lane_width_boundaries(bigint, dtype, method, n):
     B = bigint
     w = 2 if dtype == np.uint32 else 1
     bits = 8 * np.dtype(dtype).itemsize
-    for mv in (256, 257, 384, 385, 512, 513, 640, 641, 768, 769, 896, 897, 1024):
+    for mv in (256, 257, 320, 321, 384, 385, 448, 449, 512, 513, 640, 641, 768, 769, 896, 897, 1024):
         u = uniform_limbs(700 + mv, n, 2 * mv * w, dtype)
         v = uniform_limbs(701 + mv, n, mv * w, dtype)
         v[:, -1] |= 1
@@ -168,7 +168,7 @@ def test_small_lane_shape_boundaries(bigint, dtype):
     B = bigint
     w = 2 if dtype == np.uint32 else 1
     n = 2000
-    for mv in (32, 33, 48, 49, 64, 65, 96, 97, 128, 129, 192, 193):
+    for mv in (17, 24, 25, 32, 33, 48, 49, 64, 65, 96, 97, 128, 129, 192, 193):
         u = uniform_limbs(800 + mv, n, 2 * mv * w, dtype)
         v = uniform_limbs(801 + mv, n, mv * w, dtype)
         v[:, -1] |= 1
