@@ -300,7 +300,10 @@ static bi_status mul_thread_launch(const T* a, const T* b, T* r, uint32_t m, uin
     constexpr uint32_t CT = mul_thread_cta<M>();
     static const int occ = [] {
         int o = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, mul_thread_kernel<T, M, FULL>, CT, 0);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, mul_thread_kernel<T, M, FULL>, CT, 0) != cudaSuccess) {
+            cudaGetLastError();                // not the launch's error: clear it, grid one CTA an SM
+            o = 1;
+        }
         return o > 0 ? o : 1;
     }();
     const uint64_t tiles = (n + CT - 1) / CT;
